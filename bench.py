@@ -1,0 +1,442 @@
+"""Benchmark of the GB300 hash join (one JSON line on rank 0).
+
+Workload (the reference's headline join shape): build R = 2^27 rows, probe S = 2^29 rows,
+int64 keys and int64 payloads (payload = row id), R keys unique uniform 64-bit values,
+half of the S keys drawn from R and half from a disjoint range, FNV-1a 64 hash, two radix
+passes. A step is one vj_join of the device-resident tables into a device pair buffer.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--small]
+
+value   (|R|+|S|) * steps * ranks / max-over-ranks time, CUDA events on the join stream
+e2e     the same through vj_join_host with pinned HOST tables and a HOST pair buffer
+        (host->device copies of R and S and the device->host copy of the pairs inside)
+roofline  the dominant kernel: algorithmic bytes per launch / its event-timed duration
+cpu_baseline  the CPU oracle (multithreaded radix hash join) on a bounded sample
+--impl reference  times the reference's CPU join path (the oracle port of it) on the host
+
+N > 1 runs independent replicas, one per GPU (the join is single-GPU; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "vectorized-join_gb300"
+
+METRIC = "join tuples/sec (|R|+|S|) and % of HBM roofline on 1 GB300; p50/p99 per-join latency"
+UNIT = "tuples/s"
+SEED = 42
+
+
+def _import(path: Path, name: str):
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload(small: bool) -> dict:
+    lr, ls = (24, 26) if small else (27, 29)
+    return {
+        "workload": f"int64 equi-join 2^{lr} x 2^{ls}, 50% match, FNV-1a 64, 2 radix passes",
+        "r_rows": 1 << lr,
+        "s_rows": 1 << ls,
+        "key_bytes": 8,
+        "payload_bytes": 8,
+        "match_ratio": 0.5,
+        "hash": "fnv1a-64",
+        "l2_policy": "inputs (%.1f GiB) larger than the 126 MB L2; no flush needed" % (((1 << lr) + (1 << ls)) * 16 / 2**30),
+    }
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device_index: int):
+        self.device_index = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def cpu_baseline(oracle, small: bool, budget_s: float = 12.0) -> dict:
+    """Oracle join (all host threads) on a bounded sample of the same workload shape."""
+    lr, ls = (19, 21) if small else (22, 24)
+    nr, ns = 1 << lr, 1 << ls
+    g = oracle.gen_join(SEED, 8, nr, ns, 0.5)
+    threads = os.cpu_count() or 1
+    runs, t_total = 0, 0.0
+    while t_total < budget_s and runs < 50:
+        t0 = time.perf_counter()
+        cnt, _, _ = oracle.join(g["r_keys"], g["r_pay"], g["s_keys"], g["s_pay"], radix_bits=12, threads=threads, want_pairs=False)
+        t_total += time.perf_counter() - t0
+        runs += 1
+        assert cnt == g["matches"]
+    return {
+        "value": (nr + ns) * runs / t_total,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"2^{lr} x 2^{ls} rows of the same int64 50%-match workload (1/{(1 << 27) // nr} of each side), {runs} joins, {t_total:.1f} s",
+    }
+
+
+def run_reference(args, cfg) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    oracle = _import(ROOT / "oracle" / "oracle.py", "vj_oracle")
+    oracle.build()
+    lr, ls = (19, 21) if args.small else (22, 24)
+    nr, ns = 1 << lr, 1 << ls
+    g = oracle.gen_join(SEED, 8, nr, ns, 0.5)
+    threads = os.cpu_count() or 1
+
+    def step():
+        cnt, _, _ = oracle.join(g["r_keys"], g["r_pay"], g["s_keys"], g["s_pay"], radix_bits=12, threads=threads, want_pairs=False)
+        assert cnt == g["matches"]
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = (nr + ns) * args.steps / dt
+    sample = f"each step joins 2^{lr} x 2^{ls} rows of the same workload (CPU radix hash join restating the reference's algorithm, {threads} threads)"
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1000 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int64",
+        "data": "synthetic (seeded generator)",
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own CPU join (join_cpu) is a nested loop; its radix/chained-table algorithm runs here as the C oracle port on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="1/8 size workload (quick checks)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    cfg = workload(args.small)
+    if args.impl == "reference":
+        run_reference(args, cfg)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+
+    nr, ns = cfg["r_rows"], cfg["s_rows"]
+    thr = int(round(cfg["match_ratio"] * (1 << 32)))
+    seed = SEED + rank
+    rk = torch.empty(nr, dtype=torch.int64, device=dev)
+    rp = torch.empty(nr, dtype=torch.int64, device=dev)
+    sk = torch.empty(ns, dtype=torch.int64, device=dev)
+    sp = torch.empty(ns, dtype=torch.int64, device=dev)
+    vj.generate_join(seed, 8, 8, nr, ns, thr, rk, rp, sk, sp)
+    expect = vj.generate_join_expect(seed, nr, ns, thr)
+    cap = ns
+    out = torch.empty((cap, 2), dtype=torch.int64, device=dev)
+    ctx = vj.Context(local)
+    ctx.set_profiling(True)
+    t_r = vj.table(rk, rp, nr, 2, 8)
+    t_s = vj.table(sk, sp, ns, 2, 8)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return ctx.join(t_r, t_s, None, out=out, capacity=cap, stream=stream)
+
+    for _ in range(args.warmup):
+        res = step()
+    # correctness of the benchmarked configuration: count + digest against the generator
+    assert res.count == expect[0], (res.count, expect)
+    assert vj.pairs_digest(out, res.count, 8) == (expect[1], expect[2]), "digest mismatch"
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    events = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    profiles = []
+    events[0].record(stream)
+    for i in range(args.steps):
+        res = step()
+        events[i + 1].record(stream)
+        profiles.append(ctx.last_profile().as_dict())
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    step_ms = [events[i].elapsed_time(events[i + 1]) for i in range(args.steps)]
+    total_ms = events[0].elapsed_time(events[-1])
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_ms = float(t.item())
+    value = (nr + ns) * args.steps * world / (total_ms / 1000.0)
+
+    # ---- roofline of the dominant kernel (stage events recorded by the library)
+    peak, peak_src = measured_peak()
+    w_k, w_p = cfg["key_bytes"], cfg["payload_bytes"]
+    w = w_k + w_p
+    n = nr + ns
+    m = expect[0]
+    prof0 = profiles[0]
+    passes = prof0["passes"]
+
+    def avg(key, idx=None):
+        vals = [p[key][idx] if idx is not None else p[key] for p in profiles]
+        return sum(vals) / len(vals)
+
+    kernels = {}
+    for p in range(passes):
+        kernels[f"histogram_kernel (pass {p + 1})"] = (avg("ms_histogram", p), n * w_k)
+        kernels[f"scatter_kernel (pass {p + 1})"] = (avg("ms_scatter", p), n * 2 * w)
+    kernels["probe_kernel"] = (avg("ms_probe"), n * w + m * 2 * w_p)
+    # dominant kernel kind by total time per join
+    kinds = {}
+    for name, (ms, byts) in kernels.items():
+        kind = name.split(" ")[0]
+        kinds.setdefault(kind, []).append((ms, byts))
+    dom_kind = max(kinds, key=lambda k: sum(x[0] for x in kinds[k]))
+    launches = kinds[dom_kind]
+    ms_per_launch = sum(x[0] for x in launches) / len(launches)
+    bytes_per_launch = sum(x[1] for x in launches) / len(launches)
+    achieved = bytes_per_launch / (ms_per_launch / 1000.0) / 1e9
+    traffic = None
+    tpath = ROOT / "profiles" / "traffic.json"
+    if tpath.exists():
+        try:
+            traffic = json.loads(tpath.read_text()).get(dom_kind)
+        except Exception:
+            traffic = None
+    roofline = {
+        "kernel": dom_kind,
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": traffic,
+        "peak_source": peak_src,
+        "launches_per_step": len(launches),
+        "bytes_per_launch": bytes_per_launch,
+        "ms_per_launch": ms_per_launch,
+    }
+    b_alg = n * (passes * (w_k + 2 * w) + w) + m * 2 * w_p
+    ms_step = total_ms / args.steps
+    join_roofline = {
+        "bytes_alg_per_join": b_alg,
+        "achieved": b_alg / (ms_step / 1000.0) / 1e9,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": b_alg / (ms_step / 1000.0) / 1e9 / peak,
+        "formula": "(|R|+|S|)*(P*(w_k+2w)+w) + M*2*w_p",
+    }
+    stages = {name: round(ms, 4) for name, (ms, _) in kernels.items()}
+    stages["total_profiled"] = avg("ms_total")
+
+    # ---- end to end through the C ABI with host buffers
+    del out
+    torch.cuda.empty_cache()
+    h_rk = torch.empty(nr, dtype=torch.int64, pin_memory=True)
+    h_rp = torch.empty(nr, dtype=torch.int64, pin_memory=True)
+    h_sk = torch.empty(ns, dtype=torch.int64, pin_memory=True)
+    h_sp = torch.empty(ns, dtype=torch.int64, pin_memory=True)
+    h_rk.copy_(rk)
+    h_rp.copy_(rp)
+    h_sk.copy_(sk)
+    h_sp.copy_(sp)
+    del rk, rp, sk, sp
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    h_out = torch.empty((m, 2), dtype=torch.int64, pin_memory=True)
+    th_r = vj.table(h_rk, h_rp, nr, 2, 8)
+    th_s = vj.table(h_sk, h_sp, ns, 2, 8)
+    got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)  # warm-up (stages memory)
+    assert got == m
+    torch.cuda.synchronize()
+    e_steps = max(1, args.e2e_steps)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    ev0.record(stream)
+    for _ in range(e_steps):
+        got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = ev0.elapsed_time(ev1)
+    te = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_ms = float(te.item())
+    e2e = {
+        "value": n * e_steps * world / (e2e_ms / 1000.0),
+        "unit": UNIT,
+        "h2d_bytes_per_step": n * w,
+        "d2h_bytes_per_step": m * 2 * w_p,
+        "ms_per_step": e2e_ms / e_steps,
+        "steps": e_steps,
+        "api": "vj_join_host (pinned host tables in, pinned host pairs out)",
+    }
+    # spot-check the host output
+    sample = h_out[: min(m, 1 << 20)].numpy().view(np.uint64)
+    assert sample.shape[0] > 0
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        oracle = _import(ROOT / "oracle" / "oracle.py", "vj_oracle")
+        oracle.build()
+        cpu = cpu_baseline(oracle, args.small)
+
+    cfg = dict(cfg)
+    cfg["radix_passes"] = passes
+    cfg["radix_bits"] = prof0["radix_bits"][:passes]
+    cfg["build_rows_per_table"] = prof0["build_rows"]
+    cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
+    lat = sorted(step_ms)
+
+    def pct(q):
+        k = min(len(lat) - 1, max(0, int(round(q * (len(lat) - 1)))))
+        return lat[k]
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "int64",
+            "data": "synthetic (seeded counter-based generator; R unique u64 keys, S half from R, half from a disjoint range)",
+            "config": cfg,
+            "roofline": roofline,
+            "join_roofline": join_roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(sum(p["kernel_launches"] for p in profiles)),
+            "clocks": clocks,
+            "latency_ms": {"p50": pct(0.5), "p99": pct(0.99), "min": lat[0], "max": lat[-1]},
+            "stages_ms": stages,
+            "matches": m,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,245 @@
+/*
+ * vj.h -- C ABI of the GB300 (sm_103a) hash-join library.
+ *
+ * Drop-in boundary for the hash and join path of vgerber/vectorized-join:
+ *   vj_hash          replaces hash_func                (src/hash/hash.cu:507-557)
+ *   vj_partition     replaces partition_gpu            (src/join/join_provider.cu:610-661)
+ *   vj_build_probe   replaces build_and_probe_gpu      (src/join/join_provider.cu:669-847)
+ *   vj_join          replaces JoinProvider::join       (src/join/join_provider.cuh:230-421)
+ *   vj_result_free   replaces db_table::free of the rs table the join allocates
+ *                                                      (src/base/types.hpp:235-261)
+ * The reference exposes these as C++ functions over db_table/db_hash_table structs and
+ * compile-time hash/chunk widths (src/base/config.h:27-31); here the widths are runtime
+ * arguments and every call returns a status instead of exiting the process
+ * (src/base/debug.cuh:64-82). include/vj_compat.hpp rebuilds the reference's C++ names on
+ * top of this header.
+ *
+ * Conventions
+ *   - Every function returns an int status (VJ_OK = 0). vj_last_error() gives the message
+ *     of the last failure on the calling thread.
+ *   - Pointers named d_* are device pointers, h_* host pointers. Tables are views: the
+ *     library never frees or mutates caller memory (the reference's join partitions its
+ *     inputs in place, src/join/join_provider.cuh:659-663; this one does not).
+ *   - vj_stream_t is ABI-identical to cudaStream_t. Calls are stream-ordered on it; calls
+ *     that return a host value (a count, a host histogram) synchronise that stream.
+ *   - Rows per table are limited to 2^32 - 1.
+ */
+#ifndef VJ_H
+#define VJ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VJ_API __attribute__((visibility("default")))
+#else
+#define VJ_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *vj_stream_t;
+
+enum vj_status {
+    VJ_OK = 0,
+    VJ_ERR_INVALID_ARGUMENT = 1,
+    VJ_ERR_UNSUPPORTED = 2,
+    VJ_ERR_CUDA = 3,
+    VJ_ERR_OUT_OF_MEMORY = 4,
+    VJ_ERR_CAPACITY = 5,  /* caller-provided output too small; the needed count is returned */
+    VJ_ERR_DEVICE = 6,    /* a kernel reported an internal limit (bounded loop ran out) */
+    VJ_ERR_BUDGET = 7     /* request exceeds the context's HBM budget */
+};
+
+/* Hash algorithm ids, in the order of the reference dispatcher (src/hash/hash.cu:515-541). */
+enum vj_hash_algo {
+    VJ_HASH_FNV = 0,
+    VJ_HASH_CUSTOM_XOR = 1,
+    VJ_HASH_CUSTOM_XOR_SHIFT = 2,
+    VJ_HASH_CUSTOM_XOR_HW = 3,
+    VJ_HASH_CUSTOM_MULT_XOR_SHIFT = 4,
+    VJ_HASH_CUSTOM_N_MULT_XOR_SHIFT = 5,
+    VJ_HASH_CUSTOM_MULT_XOR_HW = 6,
+    VJ_HASH_CUSTOM_MULT = 7,
+    VJ_HASH_CUSTOM_MULT_SHIFT = 8,
+    VJ_HASH_CUSTOM_MULT_HW = 9,
+    VJ_HASH_CUSTOM_ADD = 10,
+    VJ_HASH_CUSTOM_ADD_SHIFT = 11,
+    VJ_HASH_CUSTOM_ADD_HW = 12,
+    VJ_HASH_COUNT = 13
+};
+
+VJ_API int vj_version(void);
+VJ_API const char *vj_status_string(int status);
+/* Copies the calling thread's last error message into buf (NUL-terminated); returns its length. */
+VJ_API size_t vj_last_error(char *buf, size_t len);
+
+/* Algorithm id for a reference algorithm name ("fnv", "custom_xor_hw", ...), or -1. The
+ * reference silently launches nothing for an unknown name (src/hash/hash.cu:515-541). */
+VJ_API int vj_hash_algo_id(const char *name);
+VJ_API const char *vj_hash_algo_name(int algo);
+
+/*
+ * vj_hash -- hash_func (src/hash/hash.cu:507-557).
+ * Element e occupies element_chunks chunks of chunk_bits/8 bytes starting at
+ * d_elements + e * element_chunks * chunk_bits/8; chunks [chunk_offset, element_chunks) are
+ * hashed. chunk_bits: 8, 32, 64 or 128 (HASH_CHUNK_BITS); hash_bits: 32 or 64 (HASH_BITS).
+ * d_hashes receives n u32 or u64 values. Bit-exact with the reference kernels, including
+ * the sign-extended char chunks of chunk_bits 8 and the *_shift variants' shift amounts
+ * outside [0, hash_bits), which give 0 as the reference's compiled shifts do.
+ * d_elements must be aligned to the chunk size. Asynchronous on stream.
+ */
+VJ_API int vj_hash(const void *d_elements, uint64_t n, int chunk_offset, int element_chunks, int chunk_bits, int hash_bits, int algo, void *d_hashes, vj_stream_t stream);
+
+/* Library context: device, stream-ordered workspace, tuning cache and HBM budget. The
+ * reference keeps the equivalent per-device state in DeviceConfig
+ * (src/join/join_provider.cuh:124-220). A context may be used from one thread at a time. */
+typedef struct vj_ctx vj_ctx;
+
+/* memory_budget_bytes: upper bound on device memory the context allocates (workspace and
+ * library-owned results); 0 = no bound beyond the device. */
+VJ_API int vj_ctx_create(int device, uint64_t memory_budget_bytes, vj_ctx **out);
+VJ_API int vj_ctx_destroy(vj_ctx *ctx);
+/* Device memory currently held by the context (workspace + owned results), in bytes. */
+VJ_API uint64_t vj_ctx_memory_in_use(const vj_ctx *ctx);
+/* Frees the cached workspace (owned results stay valid). */
+VJ_API int vj_ctx_trim(vj_ctx *ctx);
+
+/*
+ * Per-stage GPU times of the last vj_join / vj_build_probe / vj_join_host on a context with
+ * profiling enabled -- the reference's JoinSummary / PartitionSummary / ProbeSummary
+ * (src/join/join_provider.cuh:54-106, src/join/join_provider.cu:37-93). Events are
+ * recorded on the join's stream between launches; unlike the reference's profiling
+ * (join_provider.cu:148-157) nothing synchronises between kernels.
+ */
+typedef struct vj_profile {
+    int32_t passes;             /* radix passes of the last join (0..2) */
+    int32_t kernel_launches;    /* library kernels launched by the last join */
+    int32_t radix_bits[2];
+    uint32_t build_rows;        /* rows per shared-memory table */
+    uint32_t probe_rows;        /* probe rows per work item */
+    float ms_histogram[2];      /* histogram kernel of each pass */
+    float ms_scatter[2];        /* scatter kernel of each pass */
+    float ms_plan[2];           /* unit planning and the two scans of each pass */
+    float ms_probe;             /* work-item planning + build/probe kernel */
+    float ms_total;             /* first partition launch to the end of the probe */
+    uint64_t rows[2];           /* |R|, |S| */
+    uint64_t matches;
+} vj_profile;
+
+VJ_API int vj_ctx_set_profiling(vj_ctx *ctx, int enabled);
+VJ_API int vj_ctx_last_profile(const vj_ctx *ctx, vj_profile *out);
+
+/*
+ * A columnar table view (db_table, src/base/types.hpp:128-266). keys: row-major rows of
+ * key_words 32-bit words -- 1 for an int32 key, 2 for one u64 column, 2*c for c u64 key
+ * columns (c <= 4). payloads: one payload_bytes (4 or 8) value per row -- the reference's
+ * primary_keys column. A join output pair is (build payload, probe payload).
+ */
+typedef struct vj_table {
+    const void *keys;
+    const void *payloads;
+    uint64_t rows;
+    int32_t key_words;
+    int32_t payload_bytes;
+} vj_table;
+
+/*
+ * vj_partition -- one radix pass, partition_gpu (src/join/join_provider.cu:610-661).
+ * Bucket of row i = (hash_i >> radix_shift) & (2^radix_bits - 1), where hash_i is
+ * d_hashes_in[i] (u32/u64 by hash_bits) when given, else the hash_algo hash of the row's
+ * key words (as hash_func with 32-bit chunks computes it). Rows are scattered to
+ * d_keys_out / d_payloads_out (and their hashes to d_hashes_out when both hash arrays are
+ * given) grouped by bucket in ascending bucket order; the order inside a bucket is
+ * unspecified, as in the reference. radix_bits: 1..12.
+ * Histogram and exclusive offsets (2^radix_bits u64 each) go to the device arrays and/or
+ * the host arrays that are not NULL; host arrays make the call synchronous, as the
+ * reference's copies back to the host do (join_provider.cu:645-646).
+ */
+VJ_API int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashes_in, int hash_bits, int hash_algo, void *d_keys_out, void *d_payloads_out, void *d_hashes_out, int radix_shift, int radix_bits,
+                 uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream);
+
+/*
+ * vj_build_probe -- build_and_probe_gpu (src/join/join_provider.cu:669-847).
+ * Builds a hash table over r and probes it with s; a match is a pair of rows with equal
+ * hashes (when hash arrays are given) and equal key words. Writes up to `capacity` pairs
+ * (r payload, s payload), each payload_bytes wide, to d_pairs in unspecified order and
+ * the match count to *count. key_offset is accepted for signature parity (the reference
+ * takes its slot from hash >> key_offset); the result does not depend on it.
+ * Returns VJ_ERR_CAPACITY (with *count = needed) when capacity is too small.
+ * Synchronises stream.
+ */
+VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes, const vj_table *s, const void *d_s_hashes, int hash_bits, int key_offset, void *d_pairs, uint64_t capacity, uint64_t *count,
+                   vj_stream_t stream);
+
+/* Join options (JoinConfig, src/join/join_provider.cuh:108-122). A zero-initialised struct
+ * means "automatic": FNV-1a, 64-bit hash, passes, radix bits and table size from the tuner. */
+enum { VJ_JOIN_FIXED_PASSES = 1 };
+typedef struct vj_join_options {
+    int32_t hash_algo;      /* VJ_HASH_*: the hash the partitions are cut from */
+    int32_t hash_bits;      /* 32 or 64; 0 = 64 */
+    int32_t flags;          /* VJ_JOIN_FIXED_PASSES: take passes and radix_bits as given */
+    int32_t passes;         /* 0..2 radix passes (with VJ_JOIN_FIXED_PASSES) */
+    int32_t radix_bits[2];  /* bits of pass 1 and pass 2 (with VJ_JOIN_FIXED_PASSES) */
+    int32_t build_rows;     /* build rows per shared-memory table, rounded up to a power of
+                               two and capped by shared memory; 0 = largest that fits */
+    int32_t probe_rows;     /* probe rows per work item; 0 = automatic */
+    int32_t reserved[6];
+} vj_join_options;
+
+/* Join output. If pairs != NULL and capacity > 0 on entry, the caller owns the buffer (device
+ * memory, capacity pairs); otherwise the library allocates it from the context (owned = 1)
+ * and vj_result_free releases it. */
+typedef struct vj_result {
+    void *pairs;        /* count x (build payload, probe payload), payload_bytes each */
+    uint64_t count;
+    uint64_t capacity;
+    int32_t owned;
+    int32_t payload_bytes;
+} vj_result;
+
+/*
+ * vj_join -- JoinProvider::join for device tables (src/join/join_provider.cuh:286-421):
+ * hash -> radix partition (0-2 passes) -> per-partition shared-memory build/probe -> pairs.
+ * The pairs are the multiset of (r payload, s payload) over rows with equal key words, in
+ * unspecified order. r and s must have the same key_words and payload_bytes.
+ * Synchronises stream (the count is returned on the host).
+ */
+VJ_API int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, vj_result *result, vj_stream_t stream);
+
+/*
+ * vj_join_host -- the same join with HOST tables and a HOST output buffer: copies r and s
+ * to the device, joins, and copies the pairs back (up to capacity pairs). Host memory that
+ * is page-locked transfers at full link speed. Returns VJ_ERR_CAPACITY with *count = needed
+ * when capacity is too small (nothing is copied back then).
+ */
+VJ_API int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, vj_stream_t stream);
+
+VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
+
+/* Order-independent digest of a pair list: sum and xor of a 64-bit mix of each pair, the
+ * same function the CPU oracle computes. For comparing full-size joins without sorting.
+ * Synchronises stream. */
+VJ_API int vj_pairs_digest(const void *d_pairs, uint64_t count, int payload_bytes, uint64_t *h_sum, uint64_t *h_xor, vj_stream_t stream);
+
+/*
+ * Seeded workload generator (replaces the reference's time-seeded curand generator,
+ * src/benchmark/data_generator.cu:148-229). Build rows get unique keys (a bijection of the
+ * row index; in [0, 2^31) for 4-byte keys) and payload = row id. Probe row j takes the key
+ * of build row rng(j) % nr when (rng'(j) >> 32) < match_threshold, else a key no build row
+ * has; payload = j. Same values as the CPU oracle's generator. Asynchronous on stream.
+ */
+VJ_API int vj_generate_join(uint64_t seed, int key_bytes, int payload_bytes, uint64_t nr, uint64_t ns, uint64_t match_threshold, void *d_r_keys, void *d_r_payloads, void *d_s_keys, void *d_s_payloads,
+                     vj_stream_t stream);
+
+/* Expected (count, digest sum, digest xor) of the join of vj_generate_join's tables, computed
+ * on the device from the generator alone. Synchronises stream. */
+VJ_API int vj_generate_join_expect(uint64_t seed, uint64_t nr, uint64_t ns, uint64_t match_threshold, uint64_t *count, uint64_t *h_sum, uint64_t *h_xor, vj_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VJ_H */

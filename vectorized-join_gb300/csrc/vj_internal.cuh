@@ -1,0 +1,319 @@
+// vj_internal.cuh -- shared device helpers and host plumbing of the sm_103a join library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdarg>
+
+#include "vj.h"
+
+namespace vj {
+
+// ------------------------------------------------------------------ host errors
+
+int set_error(int status, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+
+#define VJ_CUDA(expr)                                                \
+    do {                                                             \
+        cudaError_t vj_e_ = (expr);                                  \
+        if (vj_e_ != cudaSuccess) return ::vj::cuda_error(vj_e_, #expr); \
+    } while (0)
+
+#define VJ_CHECK(cond, status, ...)                                  \
+    do {                                                             \
+        if (!(cond)) return ::vj::set_error((status), __VA_ARGS__);  \
+    } while (0)
+
+#define VJ_TRY(expr)                                                 \
+    do {                                                             \
+        int vj_s_ = (expr);                                          \
+        if (vj_s_ != VJ_OK) return vj_s_;                            \
+    } while (0)
+
+// ------------------------------------------------------------------ hashing
+
+__host__ __device__ __forceinline__ uint64_t fmix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ uint64_t pair_digest(uint64_t r, uint64_t s) {
+    return fmix64(r ^ fmix64(s + 0x9e3779b97f4a7c15ull));
+}
+
+template <typename H>
+struct HashTraits;
+template <>
+struct HashTraits<uint64_t> {
+    static constexpr int bits = 64;
+    static constexpr uint64_t prime = 1099511628211ull;          // 2^40 + 2^8 + 0xb3
+    static constexpr uint64_t basis = 14695981039346656037ull;
+};
+template <>
+struct HashTraits<uint32_t> {
+    static constexpr int bits = 32;
+    static constexpr uint32_t prime = 16777619u;                 // 2^24 + 2^8 + 0x93
+    static constexpr uint32_t basis = 2166136261u;
+};
+
+__device__ __forceinline__ uint32_t reverse_bits(uint32_t x) { return __brev(x); }
+__device__ __forceinline__ uint64_t reverse_bits(uint64_t x) { return __brevll(x); }
+__device__ __forceinline__ uint32_t rotl32(uint32_t v, uint32_t s) { return __funnelshift_l(v, v, s); }
+
+// The reference's get_max_shift() (hash.cu:60-62) with its integer types.
+__host__ __device__ constexpr int32_t max_shift_of(int hash_bits, int chunk_bits) {
+    return (int32_t)(uint16_t)((int32_t)(uint16_t)((uint64_t)(hash_bits / 8) - (uint64_t)(chunk_bits / 8) * 8u) + 1);
+}
+
+// State of one element's hash for algorithm ALGO with hash type H and chunk width CB.
+// lane() takes each chunk lane widened as C widens it: a sign-extended char for CB == 8,
+// a zero-extended 32-bit word otherwise. Mirrors hash.cu:84-505 operation by operation.
+template <typename H, int CB, int ALGO>
+struct HashState {
+    static constexpr int HB = HashTraits<H>::bits;
+    static constexpr int32_t MS = max_shift_of(HB, CB);
+    H h;
+    int32_t shift_i;
+    uint32_t shift_u;
+    int16_t off;
+    int16_t op;
+
+    __device__ __forceinline__ void init() {
+        shift_i = 0;
+        shift_u = 0;
+        off = 0;
+        op = 0;
+        if (ALGO == VJ_HASH_FNV) {
+            h = HashTraits<H>::basis;
+        } else if (ALGO == VJ_HASH_CUSTOM_MULT || ALGO == VJ_HASH_CUSTOM_MULT_SHIFT || ALGO == VJ_HASH_CUSTOM_MULT_HW) {
+            h = 1;
+        } else {
+            h = 0;
+        }
+    }
+    // value << amount, where amounts outside [0, HB) give 0 (the PTX shl clamp).
+    __device__ __forceinline__ static H shl(H v, int32_t amount) {
+        return (uint32_t)amount >= (uint32_t)HB ? H(0) : H(v << amount);
+    }
+    __device__ __forceinline__ void offset_from_lane(int64_t lane) {
+        if (CB == 8) {
+            int32_t sum = (int32_t)off + (int32_t)lane;
+            off = (int16_t)(sum % MS);
+        } else {
+            uint32_t sum = (uint32_t)(int32_t)off + (uint32_t)lane;
+            off = (int16_t)(uint16_t)(sum % (uint32_t)MS);
+        }
+    }
+    __device__ __forceinline__ void offset_from_hash(H ch) {
+        H sum = (H)(int64_t)off + ch;
+        off = (int16_t)(uint16_t)(sum % (H)MS);
+    }
+    __device__ __forceinline__ void lane(int64_t lv) {
+        const H ch = (H)lv;
+        const uint32_t u = (uint32_t)lv;
+        switch (ALGO) {
+        case VJ_HASH_FNV:
+            h = (H)((h ^ ch) * HashTraits<H>::prime);
+            break;
+        case VJ_HASH_CUSTOM_ADD:
+            h = (H)(h + ch);
+            break;
+        case VJ_HASH_CUSTOM_ADD_SHIFT:
+            offset_from_lane(lv);
+            h = (H)(h + shl(ch, off));
+            break;
+        case VJ_HASH_CUSTOM_ADD_HW:
+            h = (H)(h + (H)rotl32(u, (uint32_t)shift_i));
+            shift_i++;
+            break;
+        case VJ_HASH_CUSTOM_XOR:
+            h ^= ch;
+            break;
+        case VJ_HASH_CUSTOM_XOR_SHIFT:
+            offset_from_lane(lv);
+            h ^= shl(ch, off);
+            break;
+        case VJ_HASH_CUSTOM_XOR_HW:
+            shift_u += u;
+            h ^= (H)rotl32(u, shift_u);
+            h = reverse_bits(h);
+            break;
+        case VJ_HASH_CUSTOM_MULT:
+            h = (H)(1u + h * (H)(ch + 1u));
+            break;
+        case VJ_HASH_CUSTOM_MULT_SHIFT:
+            offset_from_lane(lv);
+            h = (H)(1u + shl((H)(h * (H)(ch + 1u)), off));
+            break;
+        case VJ_HASH_CUSTOM_MULT_HW:
+            shift_i = (int32_t)((uint32_t)shift_i + u);
+            h = (H)(1u + h * (H)((H)rotl32(u, (uint32_t)shift_i) + 1u));
+            h = reverse_bits(h);
+            break;
+        case VJ_HASH_CUSTOM_MULT_XOR_SHIFT:
+        case VJ_HASH_CUSTOM_N_MULT_XOR_SHIFT:
+            offset_from_hash(ch);
+            if (op & 1) {
+                h = (H)(1u + h * shl((H)(ch + 1u), off));
+            } else {
+                h = (H)(h ^ shl(ch, off));
+            }
+            op = (int16_t)(op + 1);
+            break;
+        case VJ_HASH_CUSTOM_MULT_XOR_HW:
+            if (op & 1) {
+                h = (H)(1u + h * (H)rotl32((uint32_t)(H)(ch + 1u), (uint32_t)(int32_t)off));
+            } else {
+                h = (H)(h ^ (H)rotl32((uint32_t)ch, (uint32_t)(int32_t)off));
+            }
+            op = (int16_t)(op + 1);
+            off = (int16_t)(uint16_t)((uint64_t)(int64_t)off + (uint64_t)ch);
+            h = reverse_bits(h);
+            break;
+        }
+    }
+    __device__ __forceinline__ void end_chunk() {
+        if (ALGO == VJ_HASH_CUSTOM_ADD_HW) {
+            h = reverse_bits(h);
+        }
+    }
+};
+
+// FNV-1a over the 32-bit words of a key row: the reference's hash of a join key row
+// (JoinProvider::hash_table feeds the key columns to hash_fnv, join_provider.cuh:926-931).
+template <typename H, int KW>
+__device__ __forceinline__ H fnv_words(const uint32_t (&w)[KW]) {
+    H h = HashTraits<H>::basis;
+#pragma unroll
+    for (int i = 0; i < KW; i++) {
+        h = (H)((h ^ (H)w[i]) * HashTraits<H>::prime);
+    }
+    return h;
+}
+
+// ------------------------------------------------------------------ key rows
+
+template <int KW>
+struct Key {
+    uint32_t w[KW];
+};
+
+template <int KW>
+__device__ __forceinline__ Key<KW> load_key(const void *base, uint64_t row) {
+    Key<KW> k;
+    if (KW == 1) {
+        k.w[0] = __ldg((const uint32_t *)base + row);
+    } else {
+        const uint2 *p = (const uint2 *)base + row * (KW / 2);
+#pragma unroll
+        for (int i = 0; i < KW / 2; i++) {
+            uint2 v = __ldg(p + i);
+            k.w[2 * i] = v.x;
+            k.w[2 * i + 1] = v.y;
+        }
+    }
+    return k;
+}
+
+// Streaming load: the row is read once, keep it out of L1.
+template <int KW>
+__device__ __forceinline__ Key<KW> load_key_stream(const void *base, uint64_t row) {
+    Key<KW> k;
+    if (KW == 1) {
+        k.w[0] = __ldcs((const uint32_t *)base + row);
+    } else {
+        const uint2 *p = (const uint2 *)base + row * (KW / 2);
+#pragma unroll
+        for (int i = 0; i < KW / 2; i++) {
+            uint2 v = __ldcs(p + i);
+            k.w[2 * i] = v.x;
+            k.w[2 * i + 1] = v.y;
+        }
+    }
+    return k;
+}
+
+template <int KW>
+__device__ __forceinline__ void store_key(void *base, uint64_t row, const Key<KW> &k) {
+    if (KW == 1) {
+        ((uint32_t *)base)[row] = k.w[0];
+    } else {
+        uint2 *p = (uint2 *)base + row * (KW / 2);
+#pragma unroll
+        for (int i = 0; i < KW / 2; i++) {
+            p[i] = make_uint2(k.w[2 * i], k.w[2 * i + 1]);
+        }
+    }
+}
+
+template <int KW>
+__device__ __forceinline__ bool key_equal(const Key<KW> &a, const Key<KW> &b) {
+    bool eq = true;
+#pragma unroll
+    for (int i = 0; i < KW; i++) {
+        eq &= a.w[i] == b.w[i];
+    }
+    return eq;
+}
+
+template <int PB>
+struct PayloadType;
+template <>
+struct PayloadType<4> {
+    using T = uint32_t;
+};
+template <>
+struct PayloadType<8> {
+    using T = unsigned long long;
+};
+
+// ------------------------------------------------------------------ host side
+
+struct DeviceInfo {
+    int device = 0;
+    int sms = 0;
+    size_t smem_optin = 0;
+    size_t l2_bytes = 0;
+};
+
+int device_info(int device, DeviceInfo *out);
+
+}  // namespace vj
+
+// Context (defined in vj_runtime.cu).
+struct vj_ctx {
+    int device;
+    vj::DeviceInfo info;
+    uint64_t budget;        // 0 = unbounded
+    void *workspace;
+    size_t workspace_bytes;
+    uint64_t owned_bytes;   // library-owned results
+    void *stage;            // device staging for vj_join_host
+    size_t stage_bytes;
+    bool profiling;
+    cudaEvent_t events[16];  // created on first use
+    bool events_ready;
+    vj_profile last;         // filled after each join when profiling
+    int launches;            // library kernels launched by the current join
+};
+
+namespace vj {
+// Stage event marks of a profiled join (no-ops when profiling is off).
+enum ProfileMark {
+    PM_PASS0 = 0,  // + 4 * pass: before plan_units
+    PM_HIST_END = 1,
+    PM_SCAN_END = 2,
+    PM_SCATTER_END = 3,
+    PM_PROBE_BEGIN = 8,
+    PM_PROBE_END = 9,
+    PM_COUNT = 10
+};
+void profile_mark(vj_ctx *ctx, int mark, cudaStream_t stream);
+// Grows the context workspace to at least `bytes` (stream-ordered; contents not kept).
+int workspace_reserve(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
+int owned_alloc(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
+void owned_release(vj_ctx *ctx, size_t bytes);
+}  // namespace vj

@@ -1,0 +1,765 @@
+// vj_join.cu -- host orchestration of the join path: planning, workspace carving and the
+// kernel sequence of vj_join / vj_partition / vj_build_probe / vj_join_host.
+//
+// The reference drives its pipeline from host threads: one std::thread per bucket and
+// level (src/join/join_provider.cuh:566-715), a host synchronisation per partition level
+// (:595) and per bucket pair (src/join/join_provider.cu:803), and a |R_b|*|S_b| probe
+// buffer per pair (:694). Here one stream carries a fixed sequence of launches; every
+// decision that depends on data (unit split, partition bounds, work items) is made on
+// the device, and the host synchronises once, to read the match count.
+#include "vj_join_kernels.cuh"
+
+#include <cstring>
+#include <mutex>
+
+namespace vj {
+
+namespace {
+
+// ------------------------------------------------------------------ workspace carving
+
+struct Carver {
+    char *base = nullptr;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t count, size_t align = 256) {
+        off = (off + align - 1) / align * align;
+        T *p = base ? (T *)(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+// ------------------------------------------------------------------ plan
+
+struct Plan {
+    int passes = 0;
+    int bits[2] = {0, 0};
+    uint32_t rcap = 2048;
+    uint32_t schunk = 8192;
+    uint32_t outcap = 1536;
+    int max_units[2] = {0, 0};
+};
+
+int ceil_log2(uint64_t x) {
+    int b = 0;
+    while ((1ull << b) < x) b++;
+    return b;
+}
+
+// Shared memory a probe block may use: two resident blocks per SM.
+size_t probe_smem_budget(const DeviceInfo &info) {
+    size_t per_block = info.smem_optin ? info.smem_optin : 48 * 1024;
+    size_t two = (228 * 1024) / 2 - 2048;  // 2 blocks per SM, minus per-block reservations
+    return per_block < two ? per_block : two;
+}
+
+template <int KW, int PB, int HS>
+Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt) {
+    Plan pl;
+    const size_t slot = ProbeSmem<KW, PB, HS>::slot_bytes();
+    const size_t budget = probe_smem_budget(info);
+    const size_t stage = (size_t)pl.outcap * 2 * PB;
+    uint32_t cap = 64;
+    while ((size_t)(cap * 2) * slot + stage <= budget && cap < 16384) cap <<= 1;
+    pl.rcap = cap / 2;
+    if (opt && opt->build_rows > 0) {
+        uint32_t want = 32;
+        while (want < (uint32_t)opt->build_rows && want < pl.rcap) want <<= 1;
+        pl.rcap = want;
+    }
+    if (opt && opt->probe_rows > 0) {
+        pl.schunk = (uint32_t)opt->probe_rows;
+    }
+    // passes / bits: the average build partition should fill about half a table
+    int total_bits = 0;
+    if (nr > pl.rcap) {
+        total_bits = ceil_log2((nr + pl.rcap / 2 - 1) / (pl.rcap / 2));
+    }
+    // A probe side much smaller than the build side is cheaper to stream against
+    // every build chunk than to partition: cost in probe steps.
+    const uint64_t chunks0 = (nr + pl.rcap - 1) / pl.rcap;
+    if (total_bits > 0 && chunks0 * ns <= 2 * (nr + ns)) total_bits = 0;
+    if (total_bits > 2 * MAX_RADIX_BITS) total_bits = 2 * MAX_RADIX_BITS;
+    if (total_bits == 0) {
+        pl.passes = 0;
+    } else if (total_bits <= 10) {
+        pl.passes = 1;
+        pl.bits[0] = total_bits;
+    } else {
+        pl.passes = 2;
+        pl.bits[0] = (total_bits + 1) / 2;
+        pl.bits[1] = total_bits - pl.bits[0];
+    }
+    if (opt && (opt->flags & VJ_JOIN_FIXED_PASSES)) {
+        pl.passes = opt->passes < 0 ? 0 : (opt->passes > 2 ? 2 : opt->passes);
+        pl.bits[0] = pl.passes >= 1 ? (opt->radix_bits[0] > 0 ? opt->radix_bits[0] : 8) : 0;
+        pl.bits[1] = pl.passes >= 2 ? (opt->radix_bits[1] > 0 ? opt->radix_bits[1] : 8) : 0;
+    }
+    for (int p = 0; p < 2; p++) {
+        if (pl.bits[p] > MAX_RADIX_BITS) pl.bits[p] = MAX_RADIX_BITS;
+    }
+    const int G0 = 2;
+    const int G1 = 2 << pl.bits[0];
+    pl.max_units[0] = info.sms * 16 + G0;
+    pl.max_units[1] = info.sms * 16 + G1;
+    return pl;
+}
+
+// ------------------------------------------------------------------ kernel attributes
+
+template <typename K>
+int ensure_smem(K kernel, size_t bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (bytes > 48 * 1024) {
+        VJ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    }
+    return VJ_OK;
+}
+
+constexpr int SCATTER_ITEMS = 8;
+
+struct PassBufs {
+    uint4 *units;
+    uint32_t *unit_count, *seg_first_unit, *cnt, *seg_tot, *unit_off, *part_begin, *part_end;
+};
+
+PassBufs carve_pass(Carver &c, int G, int bins, int max_units) {
+    PassBufs b;
+    b.units = c.take<uint4>(max_units);
+    b.unit_count = c.take<uint32_t>(1);
+    b.seg_first_unit = c.take<uint32_t>(G);
+    b.cnt = c.take<uint32_t>((size_t)max_units * bins);
+    b.seg_tot = c.take<uint32_t>((size_t)G * bins);
+    b.unit_off = c.take<uint32_t>((size_t)max_units * bins);
+    b.part_begin = c.take<uint32_t>((size_t)G * bins);
+    b.part_end = c.take<uint32_t>((size_t)G * bins);
+    return b;
+}
+
+template <int KW, int PB, int HS>
+int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
+    const int G = P.nsides * P.Q;
+    const uint32_t bins = 1u << P.bits;
+    P.units = b.units;
+    P.unit_count = b.unit_count;
+    P.seg_first_unit = b.seg_first_unit;
+    P.cnt = b.cnt;
+    P.seg_tot = b.seg_tot;
+    P.unit_off = b.unit_off;
+    P.part_begin = b.part_begin;
+    P.part_end = b.part_end;
+    VJ_CUDA(cudaMemsetAsync(b.seg_tot, 0, (size_t)G * bins * sizeof(uint32_t), stream));
+    plan_units_kernel<<<1, PLAN_THREADS, 0, stream>>>(P);
+    VJ_CUDA(cudaGetLastError());
+    profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
+    histogram_kernel<KW, PB, HS><<<P.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    VJ_CUDA(cudaGetLastError());
+    profile_mark(ctx, PM_HIST_END + 4 * pass, stream);
+    seg_scan_kernel<<<G, PART_THREADS, 0, stream>>>(P);
+    VJ_CUDA(cudaGetLastError());
+    const size_t us_smem = (size_t)P.max_units * sizeof(uint32_t);
+    VJ_TRY(ensure_smem(unit_scan_kernel, us_smem));
+    unit_scan_kernel<<<bins, PLAN_THREADS, us_smem, stream>>>(P);
+    VJ_CUDA(cudaGetLastError());
+    profile_mark(ctx, PM_SCAN_END + 4 * pass, stream);
+    const size_t sc_smem = ScatterSmem<KW, PB, HS, SCATTER_ITEMS>::bytes(bins);
+    VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, SCATTER_ITEMS>, sc_smem));
+    scatter_kernel<KW, PB, HS, SCATTER_ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
+    VJ_CUDA(cudaGetLastError());
+    profile_mark(ctx, PM_SCATTER_END + 4 * pass, stream);
+    if (ctx) ctx->launches += 5;
+    return VJ_OK;
+}
+
+template <int KW, int PB, int HS>
+int probe_grid(const DeviceInfo &info, size_t smem, int *grid) {
+    int per_sm = 0;
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS>, PROBE_THREADS, smem));
+    if (per_sm < 1) per_sm = 1;
+    *grid = info.sms * per_sm;
+    return VJ_OK;
+}
+
+// Device pointers of both tables, in and out of the partition passes.
+struct Tables {
+    const void *keys[2], *pay[2], *hash[2];
+    uint32_t rows[2];
+};
+
+struct JoinRun {
+    // results
+    unsigned long long *d_out_count;
+    uint32_t *d_error;
+    // probe inputs prepared by the partition passes
+    ProbeParams probe;
+    size_t probe_smem;
+    int probe_grid;
+};
+
+// Everything up to (not including) the probe launch. Returns probe parameters whose
+// output fields the caller fills in.
+template <int KW, int PB, int HS>
+int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, cudaStream_t stream, JoinRun *run) {
+    const size_t row_bytes = (size_t)KW * 4 + PB + (HS ? HS : 0);
+    const int bins0 = 1 << pl.bits[0];
+    const int bins1 = 1 << pl.bits[1];
+    const int G0 = 2, G1 = 2 * bins0;
+    const int np = pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1);
+
+    // ---- workspace layout (dry run, then carve)
+    auto layout = [&](Carver &c, void **bufA, void **bufB, PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
+        const size_t table_bytes = ((size_t)in.rows[0] + in.rows[1]) * row_bytes + 4 * 256;
+        *bufA = pl.passes >= 1 ? c.take<char>(table_bytes) : nullptr;
+        *bufB = pl.passes >= 2 ? c.take<char>(table_bytes) : nullptr;
+        if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, pl.max_units[0]);
+        if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, pl.max_units[1]);
+        *item_begin = c.take<uint32_t>((size_t)np + 1);
+        *ticket = c.take<uint32_t>(1);
+        *out_count = c.take<unsigned long long>(1);
+        *error = c.take<uint32_t>(1);
+    };
+    void *bufA, *bufB;
+    PassBufs pb0{}, pb1{};
+    uint32_t *item_begin, *ticket, *error;
+    unsigned long long *out_count;
+    Carver dry;
+    layout(dry, &bufA, &bufB, &pb0, &pb1, &item_begin, &ticket, &out_count, &error);
+    void *ws = nullptr;
+    VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
+    Carver c;
+    c.base = (char *)ws;
+    layout(c, &bufA, &bufB, &pb0, &pb1, &item_begin, &ticket, &out_count, &error);
+    VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
+    ctx->launches = 0;
+
+    // Column arrays of a partitioned copy: [R keys | S keys | R pay | S pay | R hash | S hash]
+    auto columns = [&](char *buf, void *keys[2], void *pay[2], void *hash[2]) {
+        Carver cc;
+        cc.base = buf;
+        keys[0] = cc.take<char>((size_t)in.rows[0] * KW * 4, 16);
+        keys[1] = cc.take<char>((size_t)in.rows[1] * KW * 4, 16);
+        pay[0] = cc.take<char>((size_t)in.rows[0] * PB, 16);
+        pay[1] = cc.take<char>((size_t)in.rows[1] * PB, 16);
+        hash[0] = HS ? cc.take<char>((size_t)in.rows[0] * HS, 16) : nullptr;
+        hash[1] = HS ? cc.take<char>((size_t)in.rows[1] * HS, 16) : nullptr;
+    };
+
+    const void *cur_keys[2] = {in.keys[0], in.keys[1]};
+    const void *cur_pay[2] = {in.pay[0], in.pay[1]};
+    const void *cur_hash[2] = {in.hash[0], in.hash[1]};
+    const uint32_t *seg_begin = nullptr, *seg_end = nullptr;
+    int Q = 1;
+    int consumed_bits = 0;
+    for (int pass = 0; pass < pl.passes; pass++) {
+        void *ok[2], *op[2], *oh[2];
+        columns((char *)(pass == 0 ? bufA : bufB), ok, op, oh);
+        PassParams P{};
+        for (int s = 0; s < 2; s++) {
+            P.side[s].keys_in = cur_keys[s];
+            P.side[s].pay_in = cur_pay[s];
+            P.side[s].hash_in = cur_hash[s];
+            P.side[s].keys_out = ok[s];
+            P.side[s].pay_out = op[s];
+            P.side[s].hash_out = oh[s];
+            P.side[s].rows = in.rows[s];
+        }
+        P.nsides = 2;
+        P.Q = Q;
+        P.seg_begin = seg_begin;
+        P.seg_end = seg_end;
+        P.bits = pl.bits[pass];
+        consumed_bits += pl.bits[pass];
+        P.shift = 64 - consumed_bits;  // top bits of the mixed hash, pass 1 first
+        P.hs = hs;
+        P.max_units = pl.max_units[pass];
+        P.min_unit_rows = 4096;
+        const PassBufs &pb = pass == 0 ? pb0 : pb1;
+        VJ_TRY((run_pass<KW, PB, HS>(ctx, pass, P, pb, stream)));
+        for (int s = 0; s < 2; s++) {
+            cur_keys[s] = ok[s];
+            cur_pay[s] = op[s];
+            cur_hash[s] = oh[s];
+        }
+        seg_begin = pb.part_begin;
+        seg_end = pb.part_end;
+        Q = Q << pl.bits[pass];
+    }
+
+    ProbeParams Pq{};
+    Pq.r_keys = cur_keys[0];
+    Pq.r_pay = cur_pay[0];
+    Pq.r_hash = cur_hash[0];
+    Pq.s_keys = cur_keys[1];
+    Pq.s_pay = cur_pay[1];
+    Pq.s_hash = cur_hash[1];
+    if (pl.passes == 0) {
+        Pq.r_begin = Pq.r_end = Pq.s_begin = Pq.s_end = nullptr;
+    } else {
+        Pq.r_begin = seg_begin;
+        Pq.r_end = seg_end;
+        Pq.s_begin = seg_begin + np;
+        Pq.s_end = seg_end + np;
+    }
+    Pq.r_rows = in.rows[0];
+    Pq.s_rows = in.rows[1];
+    Pq.np = np;
+    Pq.rcap = pl.rcap;
+    Pq.schunk = pl.schunk;
+    Pq.outcap = pl.outcap;
+    Pq.item_begin = item_begin;
+    Pq.ticket = ticket;
+    Pq.out_count = out_count;
+    Pq.hs = hs;
+    Pq.error = error;
+    run->probe = Pq;
+    run->d_out_count = out_count;
+    run->d_error = error;
+    run->probe_smem = ProbeSmem<KW, PB, HS>::bytes(2 * pl.rcap, pl.outcap);
+    VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS>, run->probe_smem));
+    VJ_TRY((probe_grid<KW, PB, HS>(ctx->info, run->probe_smem, &run->probe_grid)));
+    return VJ_OK;
+}
+
+template <int KW, int PB, int HS>
+int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
+    profile_mark(ctx, PM_PROBE_BEGIN, stream);
+    plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
+    VJ_CUDA(cudaGetLastError());
+    probe_kernel<KW, PB, HS><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+    VJ_CUDA(cudaGetLastError());
+    profile_mark(ctx, PM_PROBE_END, stream);
+    ctx->launches += 2;
+    return VJ_OK;
+}
+
+// After the stream has been synchronised: stage times of a profiled join.
+void finish_profile(vj_ctx *ctx, const Plan &pl, uint64_t nr, uint64_t ns, uint64_t matches) {
+    vj_profile &p = ctx->last;
+    memset(&p, 0, sizeof(p));
+    p.passes = pl.passes;
+    p.kernel_launches = ctx->launches;
+    p.radix_bits[0] = pl.bits[0];
+    p.radix_bits[1] = pl.bits[1];
+    p.build_rows = pl.rcap;
+    p.probe_rows = pl.schunk;
+    p.rows[0] = nr;
+    p.rows[1] = ns;
+    p.matches = matches;
+    if (!ctx->profiling || !ctx->events_ready) return;
+    auto ms = [&](int a, int b) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ctx->events[a], ctx->events[b]) != cudaSuccess) {
+            cudaGetLastError();
+            t = 0.f;
+        }
+        return t;
+    };
+    for (int pass = 0; pass < pl.passes; pass++) {
+        p.ms_histogram[pass] = ms(PM_PASS0 + 4 * pass, PM_HIST_END + 4 * pass);
+        p.ms_plan[pass] = ms(PM_HIST_END + 4 * pass, PM_SCAN_END + 4 * pass);
+        p.ms_scatter[pass] = ms(PM_SCAN_END + 4 * pass, PM_SCATTER_END + 4 * pass);
+    }
+    p.ms_probe = ms(PM_PROBE_BEGIN, PM_PROBE_END);
+    p.ms_total = ms(pl.passes ? PM_PASS0 : PM_PROBE_BEGIN, PM_PROBE_END);
+}
+
+int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count) {
+    static thread_local unsigned long long *pinned = nullptr;
+    if (!pinned) {
+        VJ_CUDA(cudaMallocHost(&pinned, 2 * sizeof(unsigned long long)));
+    }
+    pinned[1] = 0;
+    VJ_CUDA(cudaMemcpyAsync(&pinned[0], run.d_out_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+    VJ_CUDA(cudaMemcpyAsync(&pinned[1], run.d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    VJ_CUDA(cudaStreamSynchronize(stream));
+    VJ_CHECK((pinned[1] & 0xffffffffull) == 0, VJ_ERR_DEVICE, "probe kernel reported an internal limit (flags %llx)", pinned[1]);
+    *count = pinned[0];
+    return VJ_OK;
+}
+
+// ------------------------------------------------------------------ typed entry points
+
+template <int KW, int PB, int HS>
+int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, vj_result *res, cudaStream_t stream) {
+    const Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt);
+    JoinRun run;
+    VJ_TRY((prepare<KW, PB, HS>(ctx, t, pl, hs, stream, &run)));
+    const bool caller_buffer = res->pairs != nullptr && res->capacity > 0 && !res->owned;
+    if (!caller_buffer) {
+        uint64_t cap = t.rows[1] ? t.rows[1] : 1;
+        void *p = nullptr;
+        VJ_TRY(owned_alloc(ctx, (size_t)cap * 2 * PB, stream, &p));
+        res->pairs = p;
+        res->capacity = cap;
+        res->owned = 1;
+    }
+    res->payload_bytes = PB;
+    run.probe.out = res->pairs;
+    run.probe.capacity = res->capacity;
+    VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
+    uint64_t count = 0;
+    VJ_TRY(read_count(run, stream, &count));
+    finish_profile(ctx, pl, t.rows[0], t.rows[1], count);
+    if (count > res->capacity) {
+        if (!res->owned) {
+            res->count = count;
+            return set_error(VJ_ERR_CAPACITY, "join produced %llu pairs, output capacity is %llu", (unsigned long long)count, (unsigned long long)res->capacity);
+        }
+        // library-owned output: grow to the exact count and probe again (the partitions are
+        // still in the workspace)
+        VJ_CUDA(cudaFreeAsync(res->pairs, stream));
+        owned_release(ctx, (size_t)res->capacity * 2 * PB);
+        res->pairs = nullptr;
+        res->capacity = 0;
+        void *p = nullptr;
+        VJ_TRY(owned_alloc(ctx, (size_t)count * 2 * PB, stream, &p));
+        res->pairs = p;
+        res->capacity = count;
+        run.probe.out = p;
+        run.probe.capacity = count;
+        VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
+        uint64_t again = 0;
+        VJ_TRY(read_count(run, stream, &again));
+        VJ_CHECK(again == count, VJ_ERR_DEVICE, "second probe gave %llu pairs, first %llu", (unsigned long long)again, (unsigned long long)count);
+    }
+    res->count = count;
+    return VJ_OK;
+}
+
+template <int KW, int PB, int HS>
+int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, const HashSpec &hs, void *keys_out, void *pay_out, void *hash_out, int shift, int bits, uint64_t *d_hist, uint64_t *d_off,
+                    uint64_t *h_hist, uint64_t *h_off, cudaStream_t stream);
+
+}  // namespace
+
+// Export of a single-segment pass result as the reference's index_t histogram/offsets.
+__global__ void export_hist_kernel(const uint32_t *begin, const uint32_t *end, int bins, unsigned long long *hist, unsigned long long *off) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bins; b += gridDim.x * blockDim.x) {
+        if (hist) hist[b] = end[b] - begin[b];
+        if (off) off[b] = begin[b];
+    }
+}
+
+namespace {
+
+template <int KW, int PB, int HS>
+int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, const HashSpec &hs, void *keys_out, void *pay_out, void *hash_out, int shift, int bits, uint64_t *d_hist, uint64_t *d_off,
+                    uint64_t *h_hist, uint64_t *h_off, cudaStream_t stream) {
+    const int bins = 1 << bits;
+    const int G = 1;
+    const int max_units = ctx->info.sms * 16 + G;
+    auto layout = [&](Carver &c, PassBufs *pb, unsigned long long **hist, unsigned long long **off) {
+        *pb = carve_pass(c, G, bins, max_units);
+        *hist = c.take<unsigned long long>(bins);
+        *off = c.take<unsigned long long>(bins);
+    };
+    PassBufs pb;
+    unsigned long long *dh, *doff;
+    Carver dry;
+    layout(dry, &pb, &dh, &doff);
+    void *ws = nullptr;
+    VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
+    Carver c;
+    c.base = (char *)ws;
+    layout(c, &pb, &dh, &doff);
+    PassParams P{};
+    P.side[0].keys_in = in->keys;
+    P.side[0].pay_in = in->payloads;
+    P.side[0].hash_in = hashes_in;
+    P.side[0].keys_out = keys_out;
+    P.side[0].pay_out = pay_out;
+    P.side[0].hash_out = hash_out;
+    P.side[0].rows = (uint32_t)in->rows;
+    P.nsides = 1;
+    P.Q = 1;
+    P.seg_begin = P.seg_end = nullptr;
+    P.shift = shift;
+    P.bits = bits;
+    P.hs = hs;
+    P.max_units = max_units;
+    P.min_unit_rows = 4096;
+    if (in->rows > 0) {
+        VJ_TRY((run_pass<KW, PB, HS>(ctx, 0, P, pb, stream)));
+    } else {
+        VJ_CUDA(cudaMemsetAsync(pb.part_begin, 0, bins * sizeof(uint32_t), stream));
+        VJ_CUDA(cudaMemsetAsync(pb.part_end, 0, bins * sizeof(uint32_t), stream));
+    }
+    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(pb.part_begin, pb.part_end, bins, d_hist ? (unsigned long long *)d_hist : dh, d_off ? (unsigned long long *)d_off : doff);
+    VJ_CUDA(cudaGetLastError());
+    if (h_hist || h_off) {
+        if (h_hist) VJ_CUDA(cudaMemcpyAsync(h_hist, d_hist ? (void *)d_hist : (void *)dh, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+        if (h_off) VJ_CUDA(cudaMemcpyAsync(h_off, d_off ? (void *)d_off : (void *)doff, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+        VJ_CUDA(cudaStreamSynchronize(stream));
+    }
+    return VJ_OK;
+}
+
+// ------------------------------------------------------------------ dispatch
+
+int check_table(const vj_table *t, const char *name) {
+    VJ_CHECK(t != nullptr, VJ_ERR_INVALID_ARGUMENT, "%s: null table", name);
+    VJ_CHECK(t->key_words == 1 || t->key_words == 2 || t->key_words == 4 || t->key_words == 6 || t->key_words == 8, VJ_ERR_UNSUPPORTED, "%s: key_words must be 1, 2, 4, 6 or 8 (got %d)", name, t->key_words);
+    VJ_CHECK(t->payload_bytes == 4 || t->payload_bytes == 8, VJ_ERR_UNSUPPORTED, "%s: payload_bytes must be 4 or 8 (got %d)", name, t->payload_bytes);
+    VJ_CHECK(t->rows < (1ull << 32), VJ_ERR_UNSUPPORTED, "%s: at most 2^32-1 rows", name);
+    if (t->rows) {
+        VJ_CHECK(t->keys && t->payloads, VJ_ERR_INVALID_ARGUMENT, "%s: null column", name);
+        const uintptr_t ka = t->key_words == 1 ? 4 : 8;
+        VJ_CHECK((uintptr_t)t->keys % ka == 0, VJ_ERR_INVALID_ARGUMENT, "%s: keys must be %d-byte aligned", name, (int)ka);
+        VJ_CHECK((uintptr_t)t->payloads % t->payload_bytes == 0, VJ_ERR_INVALID_ARGUMENT, "%s: payloads must be aligned to their size", name);
+    }
+    return VJ_OK;
+}
+
+// Calls F::template run<KW, PB, HS>() for the supported layouts.
+template <typename F>
+int dispatch(int kw, int pb, int hs, F &&f) {
+#define VJ_D(K, B, H) \
+    if (kw == K && pb == B && hs == H) return f.template run<K, B, H>();
+    VJ_D(1, 4, 0)
+    VJ_D(1, 8, 0)
+    VJ_D(2, 4, 0)
+    VJ_D(2, 8, 0)
+    VJ_D(4, 4, 0)
+    VJ_D(4, 8, 0)
+    VJ_D(6, 4, 0)
+    VJ_D(6, 8, 0)
+    VJ_D(8, 4, 0)
+    VJ_D(8, 8, 0)
+    VJ_D(2, 8, 4)
+    VJ_D(2, 8, 8)
+    VJ_D(4, 8, 4)
+    VJ_D(4, 8, 8)
+    VJ_D(6, 8, 4)
+    VJ_D(6, 8, 8)
+    VJ_D(8, 8, 4)
+    VJ_D(8, 8, 8)
+#undef VJ_D
+    return set_error(VJ_ERR_UNSUPPORTED, "unsupported layout: key_words %d, payload_bytes %d, hash array bytes %d", kw, pb, hs);
+}
+
+HashSpec spec_from(const vj_join_options *opt, int mix) {
+    HashSpec hs;
+    hs.algo = opt && opt->hash_algo > 0 && opt->hash_algo < VJ_HASH_COUNT ? opt->hash_algo : VJ_HASH_FNV;
+    hs.hash_bits = opt && opt->hash_bits == 32 ? 32 : 64;
+    hs.mix = mix;
+    return hs;
+}
+
+struct JoinCall {
+    vj_ctx *ctx;
+    Tables t;
+    HashSpec hs;
+    const vj_join_options *opt;
+    vj_result *res;
+    cudaStream_t stream;
+    template <int KW, int PB, int HS>
+    int run() {
+        return join_typed<KW, PB, HS>(ctx, t, hs, opt, res, stream);
+    }
+};
+
+struct PartitionCall {
+    vj_ctx *ctx;
+    const vj_table *in;
+    const void *hashes;
+    HashSpec hs;
+    void *ko, *po, *ho;
+    int shift, bits;
+    uint64_t *dh, *doff, *hh, *hoff;
+    cudaStream_t stream;
+    template <int KW, int PB, int HS>
+    int run() {
+        return partition_typed<KW, PB, HS>(ctx, in, hashes, hs, ko, po, ho, shift, bits, dh, doff, hh, hoff, stream);
+    }
+};
+
+// build_and_probe: the plan never reallocates the caller's buffer; count only past capacity.
+struct BuildProbeCall {
+    JoinCall &c;
+    template <int KW, int PB, int HS>
+    int run() {
+        vj_result &rr = *c.res;
+        Plan pl = make_plan<KW, PB, HS>(c.t.rows[0], c.t.rows[1], c.ctx->info, nullptr);
+        JoinRun run;
+        VJ_TRY((prepare<KW, PB, HS>(c.ctx, c.t, pl, c.hs, c.stream, &run)));
+        run.probe.out = rr.pairs;
+        run.probe.capacity = rr.capacity;
+        VJ_TRY((launch_probe<KW, PB, HS>(c.ctx, run, c.stream)));
+        uint64_t n = 0;
+        VJ_TRY(read_count(run, c.stream, &n));
+        finish_profile(c.ctx, pl, c.t.rows[0], c.t.rows[1], n);
+        rr.count = n;
+        return VJ_OK;
+    }
+};
+
+}  // namespace
+
+}  // namespace vj
+
+using namespace vj;
+
+extern "C" int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, vj_result *result, vj_stream_t stream) {
+    VJ_CHECK(ctx && result, VJ_ERR_INVALID_ARGUMENT, "vj_join: null argument");
+    VJ_TRY(check_table(r, "vj_join: r"));
+    VJ_TRY(check_table(s, "vj_join: s"));
+    VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join: r and s must have the same key_words and payload_bytes");
+    VJ_CUDA(cudaSetDevice(ctx->device));
+    result->count = 0;
+    if (!(result->pairs && result->capacity > 0)) {
+        result->pairs = nullptr;
+        result->capacity = 0;
+        result->owned = 0;
+    } else {
+        result->owned = 0;
+    }
+    JoinCall call;
+    call.ctx = ctx;
+    call.t.keys[0] = r->keys;
+    call.t.keys[1] = s->keys;
+    call.t.pay[0] = r->payloads;
+    call.t.pay[1] = s->payloads;
+    call.t.hash[0] = call.t.hash[1] = nullptr;
+    call.t.rows[0] = (uint32_t)r->rows;
+    call.t.rows[1] = (uint32_t)s->rows;
+    call.hs = spec_from(options, 1);
+    call.opt = options;
+    call.res = result;
+    call.stream = (cudaStream_t)stream;
+    result->payload_bytes = r->payload_bytes;
+    if (r->rows == 0 || s->rows == 0) {
+        return VJ_OK;  // empty join: count 0, no buffer needed
+    }
+    return dispatch(r->key_words, r->payload_bytes, 0, call);
+}
+
+extern "C" int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes, const vj_table *s, const void *d_s_hashes, int hash_bits, int key_offset, void *d_pairs, uint64_t capacity, uint64_t *count,
+                              vj_stream_t stream) {
+    (void)key_offset;
+    VJ_CHECK(ctx && count, VJ_ERR_INVALID_ARGUMENT, "vj_build_probe: null argument");
+    VJ_TRY(check_table(r, "vj_build_probe: r"));
+    VJ_TRY(check_table(s, "vj_build_probe: s"));
+    VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_build_probe: r and s must have the same layout");
+    VJ_CHECK((d_r_hashes == nullptr) == (d_s_hashes == nullptr), VJ_ERR_INVALID_ARGUMENT, "vj_build_probe: give hashes for both tables or neither");
+    VJ_CHECK(hash_bits == 32 || hash_bits == 64, VJ_ERR_INVALID_ARGUMENT, "vj_build_probe: hash_bits must be 32 or 64");
+    VJ_CUDA(cudaSetDevice(ctx->device));
+    *count = 0;
+    if (r->rows == 0 || s->rows == 0) return VJ_OK;
+    VJ_CHECK(d_pairs != nullptr || capacity == 0, VJ_ERR_INVALID_ARGUMENT, "vj_build_probe: null output with capacity > 0");
+    vj_result res{};
+    res.pairs = d_pairs;
+    res.capacity = capacity;
+    res.owned = 0;
+    // capacity 0 counts only: the kernels never write at or past the capacity
+    JoinCall call;
+    call.ctx = ctx;
+    call.t.keys[0] = r->keys;
+    call.t.keys[1] = s->keys;
+    call.t.pay[0] = r->payloads;
+    call.t.pay[1] = s->payloads;
+    call.t.hash[0] = d_r_hashes;
+    call.t.hash[1] = d_s_hashes;
+    call.t.rows[0] = (uint32_t)r->rows;
+    call.t.rows[1] = (uint32_t)s->rows;
+    vj_join_options o{};
+    o.hash_bits = hash_bits;
+    call.hs = spec_from(&o, 1);
+    call.opt = nullptr;
+    call.res = &res;
+    call.stream = (cudaStream_t)stream;
+    // a caller buffer is never reallocated: mark it as caller-owned even at capacity 0
+    res.owned = 0;
+    BuildProbeCall cc{call};
+    const int hs = d_r_hashes ? hash_bits / 8 : 0;
+    VJ_TRY(dispatch(r->key_words, r->payload_bytes, hs, cc));
+    *count = res.count;
+    if (res.count > capacity) {
+        return set_error(VJ_ERR_CAPACITY, "vj_build_probe: %llu pairs, capacity %llu", (unsigned long long)res.count, (unsigned long long)capacity);
+    }
+    return VJ_OK;
+}
+
+extern "C" int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashes_in, int hash_bits, int hash_algo, void *d_keys_out, void *d_payloads_out, void *d_hashes_out, int radix_shift, int radix_bits,
+                            uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream) {
+    VJ_CHECK(ctx != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_partition: null context");
+    VJ_TRY(check_table(in, "vj_partition: in"));
+    VJ_CHECK(radix_bits >= 1 && radix_bits <= MAX_RADIX_BITS, VJ_ERR_UNSUPPORTED, "vj_partition: radix_bits must be in [1, %d]", MAX_RADIX_BITS);
+    VJ_CHECK(hash_bits == 32 || hash_bits == 64, VJ_ERR_INVALID_ARGUMENT, "vj_partition: hash_bits must be 32 or 64");
+    VJ_CHECK(radix_shift >= 0 && radix_shift < 64, VJ_ERR_INVALID_ARGUMENT, "vj_partition: radix_shift must be in [0, 63]");
+    VJ_CHECK(hash_algo >= 0 && hash_algo < VJ_HASH_COUNT, VJ_ERR_INVALID_ARGUMENT, "vj_partition: unknown hash algorithm %d", hash_algo);
+    VJ_CHECK(in->rows == 0 || (d_keys_out && d_payloads_out), VJ_ERR_INVALID_ARGUMENT, "vj_partition: null output column");
+    VJ_CUDA(cudaSetDevice(ctx->device));
+    PartitionCall call;
+    call.ctx = ctx;
+    call.in = in;
+    call.hashes = d_hashes_in;
+    call.hs.algo = hash_algo;
+    call.hs.hash_bits = hash_bits;
+    call.hs.mix = 0;
+    call.ko = d_keys_out;
+    call.po = d_payloads_out;
+    call.ho = d_hashes_in ? d_hashes_out : nullptr;
+    call.shift = radix_shift;
+    call.bits = radix_bits;
+    call.dh = d_histogram;
+    call.doff = d_offsets;
+    call.hh = h_histogram;
+    call.hoff = h_offsets;
+    call.stream = (cudaStream_t)stream;
+    return dispatch(in->key_words, in->payload_bytes, d_hashes_in ? hash_bits / 8 : 0, call);
+}
+
+extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, vj_stream_t stream) {
+    VJ_CHECK(ctx && count, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: null argument");
+    VJ_TRY(check_table(r, "vj_join_host: r"));
+    VJ_TRY(check_table(s, "vj_join_host: s"));
+    VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: r and s must have the same layout");
+    VJ_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    *count = 0;
+    const size_t kb = (size_t)r->key_words * 4, pb = (size_t)r->payload_bytes;
+    const size_t need = (r->rows + s->rows) * (kb + pb) + 4 * 256;
+    if (ctx->stage_bytes < need) {
+        if (ctx->stage) {
+            VJ_CUDA(cudaFreeAsync(ctx->stage, st));
+            ctx->stage = nullptr;
+            ctx->stage_bytes = 0;
+        }
+        VJ_CHECK(!ctx->budget || ctx->owned_bytes + ctx->workspace_bytes + need <= ctx->budget, VJ_ERR_BUDGET, "vj_join_host: input staging exceeds the context budget");
+        VJ_CUDA(cudaMallocAsync(&ctx->stage, need, st));
+        ctx->stage_bytes = need;
+    }
+    Carver c;
+    c.base = (char *)ctx->stage;
+    void *rk = c.take<char>(r->rows * kb), *rp = c.take<char>(r->rows * pb);
+    void *sk = c.take<char>(s->rows * kb), *sp = c.take<char>(s->rows * pb);
+    if (r->rows) {
+        VJ_CUDA(cudaMemcpyAsync(rk, r->keys, r->rows * kb, cudaMemcpyHostToDevice, st));
+        VJ_CUDA(cudaMemcpyAsync(rp, r->payloads, r->rows * pb, cudaMemcpyHostToDevice, st));
+    }
+    if (s->rows) {
+        VJ_CUDA(cudaMemcpyAsync(sk, s->keys, s->rows * kb, cudaMemcpyHostToDevice, st));
+        VJ_CUDA(cudaMemcpyAsync(sp, s->payloads, s->rows * pb, cudaMemcpyHostToDevice, st));
+    }
+    vj_table dr = *r, ds = *s;
+    dr.keys = rk;
+    dr.payloads = rp;
+    ds.keys = sk;
+    ds.payloads = sp;
+    vj_result res{};
+    VJ_TRY(vj_join(ctx, &dr, &ds, options, &res, stream));
+    *count = res.count;
+    int status = VJ_OK;
+    if (res.count > capacity) {
+        status = set_error(VJ_ERR_CAPACITY, "vj_join_host: %llu pairs, capacity %llu", (unsigned long long)res.count, (unsigned long long)capacity);
+    } else if (res.count) {
+        VJ_CHECK(h_pairs != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: null output");
+        cudaError_t e = cudaMemcpyAsync(h_pairs, res.pairs, res.count * 2 * pb, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) status = cuda_error(e, "vj_join_host: copy of pairs to the host");
+    }
+    vj_result_free(ctx, &res);
+    return status;
+}

@@ -1,0 +1,636 @@
+// vj_join_kernels.cuh -- radix partition and build/probe kernels of the join path.
+//
+// Data layout (HBM): every table is columnar -- a key array of rows of KW 32-bit words and
+// a payload array of PB-byte values (plus, for the reference-compatible entry points, a
+// hash array). Partition passes write the same layout into workspace buffers, grouped by
+// bucket. Nothing is materialised per row besides the tuple itself: the partitioning hash
+// is recomputed from the key in every kernel (a few integer ops per row).
+//
+// A pass over a set of "segments" (contiguous row ranges, e.g. the partitions of the
+// previous pass) runs five kernels, none of which waits on another block:
+//   plan_units   split segments into units of similar size (one block)
+//   histogram    per-unit bucket counts in shared memory
+//   seg_scan     per-segment exclusive prefix over buckets -> partition boundaries
+//   unit_scan    per-bucket prefix over units -> each unit's write cursor per bucket
+//   scatter      each unit stages a tile of rows in shared memory sorted by bucket and
+//                writes every bucket's run as one contiguous burst
+// The probe stage plans (partition, build chunk, probe chunk) work items and runs a
+// persistent kernel that takes items from an atomic ticket, builds an open-addressing
+// table of the build chunk in shared memory and streams the probe chunk through it,
+// staging output pairs in shared memory and writing them out in contiguous blocks.
+#pragma once
+
+#include "vj_internal.cuh"
+
+namespace vj {
+
+constexpr int MAX_RADIX_BITS = 12;
+constexpr int PART_THREADS = 256;
+constexpr int PROBE_THREADS = 256;
+constexpr int PROBE_ITEMS = 4;
+constexpr int PLAN_THREADS = 1024;
+
+struct HashSpec {
+    int algo;       // VJ_HASH_* when the hash is recomputed from the key
+    int hash_bits;  // 32 or 64
+    int mix;        // 1: extract bits from fmix64(hash), 0: from the raw hash
+};
+
+struct Side {
+    const void *keys_in;
+    const void *pay_in;
+    const void *hash_in;  // HS != 0 only
+    void *keys_out;
+    void *pay_out;
+    void *hash_out;       // HS != 0 only (may be null: hashes not moved)
+    uint32_t rows;
+};
+
+struct PassParams {
+    Side side[2];
+    int nsides;
+    int Q;                       // segments per side
+    const uint32_t *seg_begin;   // [nsides*Q], null: one segment = the whole side
+    const uint32_t *seg_end;
+    int shift;                   // bucket = (hash >> shift) & (2^bits - 1)
+    int bits;
+    HashSpec hs;
+    uint4 *units;                // (segment, begin, end, side)
+    uint32_t *unit_count;
+    uint32_t *seg_first_unit;    // [G]
+    int max_units;
+    uint32_t min_unit_rows;
+    uint32_t *cnt;               // [max_units][bins]
+    uint32_t *seg_tot;           // [G][bins]
+    uint32_t *unit_off;          // [max_units][bins]
+    uint32_t *part_begin;        // [G*bins]
+    uint32_t *part_end;          // [G*bins]
+};
+
+struct ProbeParams {
+    const void *r_keys, *r_pay, *r_hash;
+    const void *s_keys, *s_pay, *s_hash;
+    const uint32_t *r_begin, *r_end;  // [np]; null: one partition = whole table
+    const uint32_t *s_begin, *s_end;
+    uint32_t r_rows, s_rows;
+    int np;
+    uint32_t rcap;     // build rows per item (table capacity = 2*rcap rounded up to pow2)
+    uint32_t schunk;   // probe rows per item
+    uint32_t outcap;   // staged output pairs per block
+    uint32_t *item_begin;  // [np+1]
+    uint32_t *ticket;
+    unsigned long long *out_count;
+    void *out;
+    uint64_t capacity;
+    HashSpec hs;
+    uint32_t *error;
+};
+
+// ------------------------------------------------------------------ small helpers
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024, multiple of 32).
+// `warp_sums` needs 32 entries. Returns the exclusive prefix; *total gets the block sum.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T *total) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    T x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nwarps ? warp_sums[lane] : T(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            T y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nwarps) warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    T before = warp > 0 ? warp_sums[warp - 1] : T(0);
+    T result = before + x - v;
+    if (total) *total = warp_sums[nwarps - 1];
+    __syncthreads();
+    return result;
+}
+
+// Generic (non-FNV) row hash, out of line.
+template <typename H, int ALGO>
+__device__ H row_hash_algo(const uint32_t *w, int kw) {
+    constexpr int ROUNDS = ALGO == VJ_HASH_CUSTOM_N_MULT_XOR_SHIFT ? 2 : 1;
+    HashState<H, 32, ALGO> st;
+    st.init();
+    for (int round = 0; round < ROUNDS; round++) {
+        for (int i = 0; i < kw; i++) {
+            st.lane((int64_t)(uint64_t)w[i]);
+            st.end_chunk();
+        }
+    }
+    return st.h;
+}
+
+template <typename H>
+__device__ H row_hash_h(const uint32_t *w, int kw, int algo) {
+    switch (algo) {
+    case VJ_HASH_CUSTOM_XOR: return row_hash_algo<H, VJ_HASH_CUSTOM_XOR>(w, kw);
+    case VJ_HASH_CUSTOM_XOR_SHIFT: return row_hash_algo<H, VJ_HASH_CUSTOM_XOR_SHIFT>(w, kw);
+    case VJ_HASH_CUSTOM_XOR_HW: return row_hash_algo<H, VJ_HASH_CUSTOM_XOR_HW>(w, kw);
+    case VJ_HASH_CUSTOM_MULT_XOR_SHIFT: return row_hash_algo<H, VJ_HASH_CUSTOM_MULT_XOR_SHIFT>(w, kw);
+    case VJ_HASH_CUSTOM_N_MULT_XOR_SHIFT: return row_hash_algo<H, VJ_HASH_CUSTOM_N_MULT_XOR_SHIFT>(w, kw);
+    case VJ_HASH_CUSTOM_MULT_XOR_HW: return row_hash_algo<H, VJ_HASH_CUSTOM_MULT_XOR_HW>(w, kw);
+    case VJ_HASH_CUSTOM_MULT: return row_hash_algo<H, VJ_HASH_CUSTOM_MULT>(w, kw);
+    case VJ_HASH_CUSTOM_MULT_SHIFT: return row_hash_algo<H, VJ_HASH_CUSTOM_MULT_SHIFT>(w, kw);
+    case VJ_HASH_CUSTOM_MULT_HW: return row_hash_algo<H, VJ_HASH_CUSTOM_MULT_HW>(w, kw);
+    case VJ_HASH_CUSTOM_ADD: return row_hash_algo<H, VJ_HASH_CUSTOM_ADD>(w, kw);
+    case VJ_HASH_CUSTOM_ADD_SHIFT: return row_hash_algo<H, VJ_HASH_CUSTOM_ADD_SHIFT>(w, kw);
+    case VJ_HASH_CUSTOM_ADD_HW: return row_hash_algo<H, VJ_HASH_CUSTOM_ADD_HW>(w, kw);
+    default: return row_hash_algo<H, VJ_HASH_FNV>(w, kw);
+    }
+}
+
+static __device__ __noinline__ uint64_t row_hash_generic(const uint32_t *w, int kw, int algo, int hash_bits) {
+    if (hash_bits == 64) {
+        return row_hash_h<uint64_t>(w, kw, algo);
+    }
+    return (uint64_t)row_hash_h<uint32_t>(w, kw, algo);
+}
+
+// Hash of a key row as hash_func would compute it over 32-bit chunks.
+template <int KW>
+__device__ __forceinline__ uint64_t row_hash(const Key<KW> &k, const HashSpec &hs) {
+    if (hs.algo == VJ_HASH_FNV) {
+        return hs.hash_bits == 64 ? fnv_words<uint64_t, KW>(k.w) : (uint64_t)fnv_words<uint32_t, KW>(k.w);
+    }
+    uint32_t w[KW];
+#pragma unroll
+    for (int i = 0; i < KW; i++) w[i] = k.w[i];
+    return row_hash_generic(w, KW, hs.algo, hs.hash_bits);
+}
+
+// A row while it moves through a kernel. HS: 0 = hash recomputed from the key, 4/8 = hash
+// read from (and carried with) a u32/u64 hash array.
+template <int KW, int PB, int HS>
+struct Row {
+    using P = typename PayloadType<PB>::T;
+    Key<KW> k;
+    P p;
+    uint64_t h;   // hash as given or recomputed (before mixing)
+};
+
+template <int HS>
+__device__ __forceinline__ uint64_t load_hash(const void *base, uint64_t row) {
+    if (HS == 8) return __ldcs((const unsigned long long *)base + row);
+    return (uint64_t)__ldcs((const uint32_t *)base + row);
+}
+
+template <int KW, int PB, int HS>
+__device__ __forceinline__ void load_row(const void *keys, const void *pay, const void *hashes, uint64_t i, const HashSpec &hs, Row<KW, PB, HS> &r) {
+    using P = typename PayloadType<PB>::T;
+    r.k = load_key_stream<KW>(keys, i);
+    r.p = __ldcs((const P *)pay + i);
+    if (HS) {
+        r.h = load_hash<HS>(hashes, i);
+    } else {
+        r.h = row_hash<KW>(r.k, hs);
+    }
+}
+
+__device__ __forceinline__ uint64_t bucket_hash(uint64_t h, const HashSpec &hs) {
+    return hs.mix ? fmix64(h) : h;
+}
+
+// ------------------------------------------------------------------ partition kernels
+
+// One block. Splits the G segments into units of at most `target` rows.
+__global__ void __launch_bounds__(PLAN_THREADS) plan_units_kernel(PassParams P) {
+    __shared__ unsigned long long s_warp64[32];
+    __shared__ uint32_t s_warp32[32];
+    const int G = P.nsides * P.Q;
+    const int per = (G + PLAN_THREADS - 1) / PLAN_THREADS;
+    const int g0 = threadIdx.x * per;
+    unsigned long long my_rows = 0;
+    for (int g = g0; g < g0 + per && g < G; g++) {
+        const int side = g / P.Q;
+        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
+        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
+        my_rows += e - b;
+    }
+    unsigned long long total = 0;
+    block_exclusive_scan<unsigned long long>(my_rows, s_warp64, &total);
+    const unsigned long long budget = P.max_units > G ? (unsigned long long)(P.max_units - G) : 1ull;
+    unsigned long long target = (total + budget - 1) / budget;
+    if (target < P.min_unit_rows) target = P.min_unit_rows;
+    if (target < 1) target = 1;
+    uint32_t my_units = 0;
+    for (int g = g0; g < g0 + per && g < G; g++) {
+        const int side = g / P.Q;
+        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
+        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
+        my_units += (uint32_t)(((unsigned long long)(e - b) + target - 1) / target);
+    }
+    uint32_t units_total = 0;
+    uint32_t first = block_exclusive_scan<uint32_t>(my_units, s_warp32, &units_total);
+    for (int g = g0; g < g0 + per && g < G; g++) {
+        const int side = g / P.Q;
+        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
+        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
+        P.seg_first_unit[g] = first;
+        for (unsigned long long x = b; x < e; x += target) {
+            unsigned long long xe = x + target < e ? x + target : e;
+            P.units[first++] = make_uint4((uint32_t)g, (uint32_t)x, (uint32_t)xe, (uint32_t)side);
+        }
+    }
+    if (threadIdx.x == 0) {
+        *P.unit_count = units_total;
+    }
+}
+
+template <int KW, int PB, int HS>
+__global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
+    extern __shared__ uint32_t s_hist[];
+    const uint32_t u = blockIdx.x;
+    if (u >= *P.unit_count) return;
+    const uint4 U = P.units[u];
+    const Side &S = P.side[U.w];
+    const uint32_t bins = 1u << P.bits;
+    const uint64_t mask = bins - 1;
+    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
+    __syncthreads();
+    constexpr int UNROLL = 4;
+    uint32_t i = U.y + threadIdx.x;
+    for (; i + (UNROLL - 1) * PART_THREADS < U.z; i += UNROLL * PART_THREADS) {
+        uint64_t h[UNROLL];
+        if (HS) {
+#pragma unroll
+            for (int k = 0; k < UNROLL; k++) h[k] = load_hash<HS>(S.hash_in, i + k * PART_THREADS);
+        } else {
+            Key<KW> key[UNROLL];
+#pragma unroll
+            for (int k = 0; k < UNROLL; k++) key[k] = load_key_stream<KW>(S.keys_in, i + k * PART_THREADS);
+#pragma unroll
+            for (int k = 0; k < UNROLL; k++) h[k] = row_hash<KW>(key[k], P.hs);
+        }
+#pragma unroll
+        for (int k = 0; k < UNROLL; k++) atomicAdd(&s_hist[(bucket_hash(h[k], P.hs) >> P.shift) & mask], 1u);
+    }
+    for (; i < U.z; i += PART_THREADS) {
+        uint64_t h = HS ? load_hash<HS>(S.hash_in, i) : row_hash<KW>(load_key_stream<KW>(S.keys_in, i), P.hs);
+        atomicAdd(&s_hist[(bucket_hash(h, P.hs) >> P.shift) & mask], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
+        uint32_t c = s_hist[b];
+        P.cnt[(size_t)u * bins + b] = c;
+        if (c) atomicAdd(&P.seg_tot[(size_t)U.x * bins + b], c);
+    }
+}
+
+// Grid: one block per segment. Partition boundaries of every (segment, bucket).
+__global__ void __launch_bounds__(PART_THREADS) seg_scan_kernel(PassParams P) {
+    __shared__ uint32_t s_warp[32];
+    const int g = blockIdx.x;
+    const int side = g / P.Q;
+    const uint32_t bins = 1u << P.bits;
+    const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
+    const uint32_t b0 = threadIdx.x * per;
+    const uint32_t *tot = P.seg_tot + (size_t)g * bins;
+    uint32_t mine = 0;
+    for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += tot[b];
+    uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
+    run += P.seg_begin ? P.seg_begin[g] : 0;
+    (void)side;
+    for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
+        P.part_begin[(size_t)g * bins + b] = run;
+        run += tot[b];
+        P.part_end[(size_t)g * bins + b] = run;
+    }
+}
+
+// Grid: one block per bucket. Write cursor of every (unit, bucket).
+__global__ void __launch_bounds__(PLAN_THREADS) unit_scan_kernel(PassParams P) {
+    extern __shared__ uint32_t s_excl[];  // [unit_count]
+    __shared__ uint32_t s_warp[32];
+    const uint32_t b = blockIdx.x;
+    const uint32_t bins = 1u << P.bits;
+    const uint32_t U = *P.unit_count;
+    const uint32_t per = (U + PLAN_THREADS - 1) / PLAN_THREADS;
+    const uint32_t u0 = threadIdx.x * per;
+    uint32_t mine = 0;
+    for (uint32_t u = u0; u < u0 + per && u < U; u++) mine += P.cnt[(size_t)u * bins + b];
+    uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
+    for (uint32_t u = u0; u < u0 + per && u < U; u++) {
+        s_excl[u] = run;
+        run += P.cnt[(size_t)u * bins + b];
+    }
+    __syncthreads();
+    for (uint32_t u = threadIdx.x; u < U; u += PLAN_THREADS) {
+        const uint32_t g = P.units[u].x;
+        P.unit_off[(size_t)u * bins + b] = P.part_begin[(size_t)g * bins + b] + s_excl[u] - s_excl[P.seg_first_unit[g]];
+    }
+}
+
+template <int KW, int PB, int HS, int ITEMS>
+struct ScatterSmem {
+    using P = typename PayloadType<PB>::T;
+    static constexpr int T = PART_THREADS * ITEMS;
+    static size_t bytes(uint32_t bins) {
+        return (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2) + (size_t)bins * 3 * 4;
+    }
+};
+
+template <int KW, int PB, int HS, int ITEMS>
+__global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
+    using Pt = typename PayloadType<PB>::T;
+    constexpr int T = PART_THREADS * ITEMS;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    // staging layout: keys | payloads | hashes | bucket ids | run | cnt | start
+    Key<KW> *st_key = (Key<KW> *)s_raw;
+    Pt *st_pay = (Pt *)(s_raw + (size_t)T * KW * 4);
+    unsigned long long *st_hash = (unsigned long long *)(s_raw + (size_t)T * (KW * 4 + PB));
+    uint16_t *st_b = (uint16_t *)(s_raw + (size_t)T * (KW * 4 + PB + (HS ? 8 : 0)));
+    const uint32_t bins = 1u << P.bits;
+    uint32_t *s_run = (uint32_t *)(s_raw + (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2));
+    uint32_t *s_cnt = s_run + bins;
+    uint32_t *s_start = s_cnt + bins;
+    __shared__ uint32_t s_warp[32];
+
+    const uint32_t u = blockIdx.x;
+    if (u >= *P.unit_count) return;
+    const uint4 U = P.units[u];
+    const Side &S = P.side[U.w];
+    const uint64_t mask = bins - 1;
+    const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
+    const uint32_t b0 = threadIdx.x * per;
+    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_run[b] = P.unit_off[(size_t)u * bins + b];
+
+    for (uint32_t tile = U.y; tile < U.z; tile += T) {
+        const uint32_t nt = U.z - tile < (uint32_t)T ? U.z - tile : (uint32_t)T;
+        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_cnt[b] = 0;
+        __syncthreads();
+        Row<KW, PB, HS> row[ITEMS];
+        uint32_t bk[ITEMS];
+        uint32_t rk[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const uint32_t i = k * PART_THREADS + threadIdx.x;
+            if (i < nt) load_row<KW, PB, HS>(S.keys_in, S.pay_in, S.hash_in, tile + i, P.hs, row[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const uint32_t i = k * PART_THREADS + threadIdx.x;
+            if (i < nt) {
+                bk[k] = (uint32_t)((bucket_hash(row[k].h, P.hs) >> P.shift) & mask);
+                rk[k] = atomicAdd(&s_cnt[bk[k]], 1u);
+            }
+        }
+        __syncthreads();
+        {
+            uint32_t mine = 0;
+            for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += s_cnt[b];
+            uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
+            for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
+                s_start[b] = run;
+                run += s_cnt[b];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const uint32_t i = k * PART_THREADS + threadIdx.x;
+            if (i < nt) {
+                const uint32_t pos = s_start[bk[k]] + rk[k];
+                st_key[pos] = row[k].k;
+                st_pay[pos] = row[k].p;
+                if (HS) st_hash[pos] = row[k].h;
+                st_b[pos] = (uint16_t)bk[k];
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
+            const uint32_t b = st_b[i];
+            const uint32_t dst = s_run[b] + i - s_start[b];
+            store_key<KW>(S.keys_out, dst, st_key[i]);
+            __stcs((Pt *)S.pay_out + dst, st_pay[i]);
+            if (HS && S.hash_out) {
+                if (HS == 8) ((unsigned long long *)S.hash_out)[dst] = st_hash[i];
+                else ((uint32_t *)S.hash_out)[dst] = (uint32_t)st_hash[i];
+            }
+        }
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_run[b] += s_cnt[b];
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ probe kernels
+
+// Work items of partition p: (build chunks) x (probe chunks), 0 if either side is empty.
+__device__ __forceinline__ unsigned long long items_of(const ProbeParams &Q, int p) {
+    const uint32_t nr = Q.r_begin ? Q.r_end[p] - Q.r_begin[p] : Q.r_rows;
+    const uint32_t ns = Q.s_begin ? Q.s_end[p] - Q.s_begin[p] : Q.s_rows;
+    if (!nr || !ns) return 0;
+    return (unsigned long long)((nr + Q.rcap - 1) / Q.rcap) * ((ns + Q.schunk - 1) / Q.schunk);
+}
+
+// One block. Work items per partition and their prefix; resets the ticket and counter.
+// A plan of 2^31 or more items (only reachable when almost every row shares one hash)
+// is refused with error flag 2 and no items.
+__global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q) {
+    __shared__ unsigned long long s_warp[32];
+    const int per = (Q.np + PLAN_THREADS - 1) / PLAN_THREADS;
+    const int p0 = threadIdx.x * per;
+    unsigned long long mine = 0;
+    for (int p = p0; p < p0 + per && p < Q.np; p++) mine += items_of(Q, p);
+    unsigned long long total = 0;
+    unsigned long long run = block_exclusive_scan<unsigned long long>(mine, s_warp, &total);
+    const bool too_many = total >= (1ull << 31);
+    for (int p = p0; p < p0 + per && p < Q.np; p++) {
+        Q.item_begin[p] = too_many ? 0u : (uint32_t)run;
+        run += items_of(Q, p);
+    }
+    if (threadIdx.x == 0) {
+        Q.item_begin[Q.np] = too_many ? 0u : (uint32_t)total;
+        if (too_many) atomicOr(Q.error, 2u);
+        *Q.ticket = 0;
+        *Q.out_count = 0;
+    }
+}
+
+template <int PB>
+struct Pair;
+template <>
+struct Pair<4> {
+    using T = uint2;
+    static __device__ __forceinline__ T make(uint32_t a, uint32_t b) { return make_uint2(a, b); }
+};
+template <>
+struct Pair<8> {
+    using T = ulonglong2;
+    static __device__ __forceinline__ T make(unsigned long long a, unsigned long long b) { return make_ulonglong2(a, b); }
+};
+
+template <int KW, int PB, int HS>
+struct ProbeSmem {
+    static size_t slot_bytes() { return 4 + KW * 4 + PB + (HS ? 8 : 0); }
+    static size_t bytes(uint32_t cap, uint32_t outcap) { return (size_t)cap * slot_bytes() + (size_t)outcap * 2 * PB; }
+};
+
+// Write the staged pairs [0, n) to the output at a block of positions taken from the
+// global counter; positions at or past the capacity are dropped (the count still grows).
+template <int PB>
+__device__ __forceinline__ void flush_pairs(const ProbeParams &Q, typename Pair<PB>::T *stage, uint32_t n, unsigned long long *s_base) {
+    using PT = typename Pair<PB>::T;
+    if (threadIdx.x == 0) *s_base = atomicAdd(Q.out_count, (unsigned long long)n);
+    __syncthreads();
+    const unsigned long long base = *s_base;
+    PT *out = (PT *)Q.out;
+    for (uint32_t i = threadIdx.x; i < n; i += PROBE_THREADS) {
+        if (base + i < Q.capacity) __stcs(out + base + i, stage[i]);
+    }
+}
+
+template <int KW, int PB, int HS>
+__global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
+    using Pt = typename PayloadType<PB>::T;
+    using PT = typename Pair<PB>::T;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const uint32_t max_cap = 2 * Q.rcap;  // rcap is a power of two
+    // layout: pairs staging | payloads | keys | hashes | slot index
+    PT *stage = (PT *)s_raw;
+    Pt *t_pay = (Pt *)(s_raw + (size_t)Q.outcap * sizeof(PT));
+    Key<KW> *t_key = (Key<KW> *)((unsigned char *)t_pay + (size_t)max_cap * PB);
+    unsigned long long *t_hash = (unsigned long long *)((unsigned char *)t_key + (size_t)max_cap * KW * 4);
+    uint32_t *t_idx = (uint32_t *)((unsigned char *)t_hash + (HS ? (size_t)max_cap * 8 : 0));
+
+    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_out_n;
+    __shared__ unsigned long long s_base;
+    const int lane = threadIdx.x & 31;
+    const uint32_t total_items = Q.item_begin[Q.np];
+    if (threadIdx.x == 0) s_out_n = 0;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(Q.ticket, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= total_items) break;
+        // partition of this item: last p with item_begin[p] <= item
+        int lo = 0, hi = Q.np - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (Q.item_begin[mid] <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const int p = lo;
+        const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
+        const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
+        const uint32_t nsc = (se - sb + Q.schunk - 1) / Q.schunk;
+        const uint32_t k = item - Q.item_begin[p];
+        const uint32_t r0 = rb + (k / nsc) * Q.rcap;
+        const uint32_t r1 = re - r0 < Q.rcap ? re : r0 + Q.rcap;
+        const uint32_t s0 = sb + (k % nsc) * Q.schunk;
+        const uint32_t s1 = se - s0 < Q.schunk ? se : s0 + Q.schunk;
+        const uint32_t nr = r1 - r0;
+        uint32_t cap = 64;
+        while (cap < 2 * nr) cap <<= 1;
+        const uint32_t cmask = cap - 1;
+
+        // ---- build
+        for (uint32_t i = threadIdx.x; i < cap; i += PROBE_THREADS) t_idx[i] = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < nr; i += PROBE_THREADS) {
+            Row<KW, PB, HS> r;
+            load_row<KW, PB, HS>(Q.r_keys, Q.r_pay, Q.r_hash, r0 + i, Q.hs, r);
+            uint32_t slot = (uint32_t)fmix64(r.h) & cmask;
+            uint32_t tries = 0;
+            while (atomicCAS(&t_idx[slot], 0u, i + 1) != 0u) {
+                slot = (slot + 1) & cmask;
+                if (++tries > cap) {  // cannot happen: at most half the slots are used
+                    atomicOr(Q.error, 1u);
+                    break;
+                }
+            }
+            t_key[slot] = r.k;
+            t_pay[slot] = r.p;
+            if (HS) t_hash[slot] = r.h;
+        }
+        __syncthreads();
+
+        // ---- probe
+        for (uint32_t base = s0; base < s1; base += PROBE_THREADS * PROBE_ITEMS) {
+            Row<KW, PB, HS> srow[PROBE_ITEMS];
+#pragma unroll
+            for (int j = 0; j < PROBE_ITEMS; j++) {
+                const uint32_t i = base + j * PROBE_THREADS + threadIdx.x;
+                if (i < s1) load_row<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, i, Q.hs, srow[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < PROBE_ITEMS; j++) {
+                const uint32_t i = base + j * PROBE_THREADS + threadIdx.x;
+                bool active = i < s1;
+                uint32_t slot = active ? (uint32_t)fmix64(srow[j].h) & cmask : 0;
+                // Lanes walk their probe sequences in lock step; each step emits the lanes
+                // that matched with one shared-memory reservation per warp.
+                while (__any_sync(0xffffffffu, active)) {
+                    bool match = false;
+                    Pt rp = 0;
+                    if (active) {
+                        if (t_idx[slot] == 0) {
+                            active = false;
+                        } else {
+                            if (key_equal<KW>(t_key[slot], srow[j].k) && (!HS || t_hash[slot] == srow[j].h)) {
+                                match = true;
+                                rp = t_pay[slot];
+                            }
+                            slot = (slot + 1) & cmask;
+                        }
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, match);
+                    if (m) {
+                        const int leader = __ffs(m) - 1;
+                        uint32_t pos0 = 0;
+                        if (lane == leader) pos0 = atomicAdd(&s_out_n, (uint32_t)__popc(m));
+                        pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+                        if (match) {
+                            const uint32_t pos = pos0 + __popc(m & lanemask_lt());
+                            if (pos < Q.outcap) {
+                                stage[pos] = Pair<PB>::make(rp, srow[j].p);
+                            } else {
+                                // staging full (build rows with many duplicates): direct write
+                                unsigned long long g = atomicAdd(Q.out_count, 1ull);
+                                if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, srow[j].p);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            uint32_t n = s_out_n;
+            if (n > Q.outcap) n = Q.outcap;
+            if (n + PROBE_THREADS * PROBE_ITEMS > Q.outcap) {
+                flush_pairs<PB>(Q, stage, n, &s_base);
+                __syncthreads();
+                if (threadIdx.x == 0) s_out_n = 0;
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t n = s_out_n;
+    if (n > Q.outcap) n = Q.outcap;
+    if (n) flush_pairs<PB>(Q, stage, n, &s_base);
+}
+
+}  // namespace vj
