@@ -247,7 +247,11 @@ def stream_handle(stream=None) -> int | None:
 
 
 def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTable:
-    return VjTable(ptr(keys), ptr(payloads), rows, key_words, payload_bytes)
+    """A vj_table view. The view keeps `keys` and `payloads` alive: a view of temporaries
+    would otherwise point at memory the allocator hands out again."""
+    t = VjTable(ptr(keys), ptr(payloads), rows, key_words, payload_bytes)
+    t._refs = (keys, payloads)
+    return t
 
 
 def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0) -> VjJoinOptions:
