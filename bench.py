@@ -47,8 +47,8 @@ def _import(path: Path, name: str):
     return mod
 
 
-def workload(small: bool) -> dict:
-    lr, ls = (24, 26) if small else (27, 29)
+def workload(shift: int) -> dict:
+    lr, ls = 27 - shift, 29 - shift
     return {
         "workload": f"int64 equi-join 2^{lr} x 2^{ls}, 50% match, FNV-1a 64, 2 radix passes",
         "r_rows": 1 << lr,
@@ -200,18 +200,71 @@ def run_reference(args, cfg) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_e2e(args, ctx, vj, torch, stream, dev, world, rk, rp, sk, sp, nr, ns, m, w, w_p):
+    """The same join through vj_join_host: pinned host tables in, pinned host pairs out."""
+    import torch.distributed as dist
+
+    n = nr + ns
+    torch.cuda.empty_cache()
+    h_rk = torch.empty(nr, dtype=torch.int64, pin_memory=True)
+    h_rp = torch.empty(nr, dtype=torch.int64, pin_memory=True)
+    h_sk = torch.empty(ns, dtype=torch.int64, pin_memory=True)
+    h_sp = torch.empty(ns, dtype=torch.int64, pin_memory=True)
+    h_rk.copy_(rk)
+    h_rp.copy_(rp)
+    h_sk.copy_(sk)
+    h_sp.copy_(sp)
+    torch.cuda.synchronize()
+    h_out = torch.empty((m, 2), dtype=torch.int64, pin_memory=True)
+    th_r = vj.table(h_rk, h_rp, nr, 2, 8)
+    th_s = vj.table(h_sk, h_sp, ns, 2, 8)
+    got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)  # warm-up (allocates the staging buffer)
+    assert got == m
+    torch.cuda.synchronize()
+    e_steps = max(1, args.e2e_steps)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    ev0.record(stream)
+    for _ in range(e_steps):
+        got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    assert got == m
+    e2e_ms = ev0.elapsed_time(ev1)
+    te = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_ms = float(te.item())
+    return {
+        "value": n * e_steps * world / (e2e_ms / 1000.0),
+        "unit": UNIT,
+        "h2d_bytes_per_step": n * w,
+        "d2h_bytes_per_step": m * 2 * w_p,
+        "ms_per_step": e2e_ms / e_steps,
+        "steps": e_steps,
+        "api": "vj_join_host (pinned host tables in, pinned host pairs out)",
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--small", action="store_true", help="1/8 size workload (quick checks)")
+    ap.add_argument("--small", action="store_true", help="1/8 size workload (quick checks), same as --shift 3")
+    ap.add_argument("--shift", type=int, default=0, help="divide both table sizes by 2^shift (profiling cases)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    cfg = workload(args.small)
+    if args.small:
+        args.shift = max(args.shift, 3)
+    args.small = args.shift > 0
+    cfg = workload(args.shift)
     if args.impl == "reference":
         run_reference(args, cfg)
         return
@@ -344,51 +397,12 @@ def main():
 
     # ---- end to end through the C ABI with host buffers
     del out
-    torch.cuda.empty_cache()
-    h_rk = torch.empty(nr, dtype=torch.int64, pin_memory=True)
-    h_rp = torch.empty(nr, dtype=torch.int64, pin_memory=True)
-    h_sk = torch.empty(ns, dtype=torch.int64, pin_memory=True)
-    h_sp = torch.empty(ns, dtype=torch.int64, pin_memory=True)
-    h_rk.copy_(rk)
-    h_rp.copy_(rp)
-    h_sk.copy_(sk)
-    h_sp.copy_(sp)
-    del rk, rp, sk, sp
-    torch.cuda.synchronize()
-    torch.cuda.empty_cache()
-    h_out = torch.empty((m, 2), dtype=torch.int64, pin_memory=True)
-    th_r = vj.table(h_rk, h_rp, nr, 2, 8)
-    th_s = vj.table(h_sk, h_sp, ns, 2, 8)
-    got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)  # warm-up (stages memory)
-    assert got == m
-    torch.cuda.synchronize()
-    e_steps = max(1, args.e2e_steps)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        dist.barrier()
-    ev0.record(stream)
-    for _ in range(e_steps):
-        got = ctx.join_host(th_r, th_s, h_out, m, stream=stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = ev0.elapsed_time(ev1)
-    te = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_ms = float(te.item())
-    e2e = {
-        "value": n * e_steps * world / (e2e_ms / 1000.0),
-        "unit": UNIT,
-        "h2d_bytes_per_step": n * w,
-        "d2h_bytes_per_step": m * 2 * w_p,
-        "ms_per_step": e2e_ms / e_steps,
-        "steps": e_steps,
-        "api": "vj_join_host (pinned host tables in, pinned host pairs out)",
-    }
-    # spot-check the host output
-    sample = h_out[: min(m, 1 << 20)].numpy().view(np.uint64)
-    assert sample.shape[0] > 0
+    e2e = None
+    if args.no_e2e:
+        del rk, rp, sk, sp
+    else:
+        e2e = run_e2e(args, ctx, vj, torch, stream, dev, world, rk, rp, sk, sp, nr, ns, m, w, w_p)
+        del rk, rp, sk, sp
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -270,6 +270,103 @@ struct PayloadType<8> {
     using T = unsigned long long;
 };
 
+// ------------------------------------------------------------------ bulk copies (TMA engine)
+//
+// 1-D global->shared copies by the Blackwell bulk-copy (TMA) engine, completing on an
+// mbarrier with a transaction count. Every wait is bounded: after WAIT_LIMIT polls the
+// caller gets `false` and is expected to flag the error and leave.
+
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes mbarrier initialisation and earlier generic-proxy accesses of shared memory
+// visible to the async proxy (issue before handing a buffer to a bulk copy).
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+    }
+    return false;
+}
+
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// The 16-byte aligned window of global memory that covers rows [a, b) of a column with
+// `cb`-byte rows starting at `base`. Bytes outside the column inside that window share a
+// 16-byte chunk with column bytes, so reading them cannot cross a page boundary.
+struct ColWindow {
+    const unsigned char *src;  // window start (16-byte aligned)
+    uint32_t bytes;            // window size (multiple of 16)
+    uint32_t delta;            // offset of row a inside the window
+};
+
+__device__ __forceinline__ ColWindow col_window(const void *base, uint32_t cb, uint32_t a, uint32_t b) {
+    const uintptr_t lo = (uintptr_t)base + (uintptr_t)a * cb;
+    const uintptr_t hi = (uintptr_t)base + (uintptr_t)b * cb;
+    const uintptr_t wlo = lo & ~(uintptr_t)15;
+    const uintptr_t whi = (hi + 15) & ~(uintptr_t)15;
+    ColWindow w;
+    w.src = (const unsigned char *)wlo;
+    w.bytes = (uint32_t)(whi - wlo);
+    w.delta = (uint32_t)(lo - wlo);
+    return w;
+}
+
+// Key of KW words at byte address p in shared memory (p aligned to 8 for KW >= 2, 4 for KW 1).
+template <int KW>
+__device__ __forceinline__ Key<KW> key_from_smem(const unsigned char *p) {
+    Key<KW> k;
+    if (KW == 1) {
+        k.w[0] = *(const uint32_t *)p;
+    } else {
+#pragma unroll
+        for (int i = 0; i < KW / 2; i++) {
+            uint2 v = ((const uint2 *)p)[i];
+            k.w[2 * i] = v.x;
+            k.w[2 * i + 1] = v.y;
+        }
+    }
+    return k;
+}
+
+template <int KW>
+__device__ __forceinline__ void key_to_smem(unsigned char *p, const Key<KW> &k) {
+    if (KW == 1) {
+        *(uint32_t *)p = k.w[0];
+    } else {
+#pragma unroll
+        for (int i = 0; i < KW / 2; i++) ((uint2 *)p)[i] = make_uint2(k.w[2 * i], k.w[2 * i + 1]);
+    }
+}
+
 // ------------------------------------------------------------------ host side
 
 struct DeviceInfo {

@@ -35,9 +35,10 @@ struct Carver {
 struct Plan {
     int passes = 0;
     int bits[2] = {0, 0};
-    uint32_t rcap = 2048;
-    uint32_t schunk = 8192;
-    uint32_t outcap = 1536;
+    uint32_t rcap = 2048;     // build rows per table
+    uint32_t schunk = 8192;   // probe rows per work item
+    uint32_t sub = 1024;      // probe rows per bulk copy
+    uint32_t outcap = 1536;   // staged output pairs per block
     int max_units[2] = {0, 0};
 };
 
@@ -57,12 +58,21 @@ size_t probe_smem_budget(const DeviceInfo &info) {
 template <int KW, int PB, int HS>
 Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt) {
     Plan pl;
-    const size_t slot = ProbeSmem<KW, PB, HS>::slot_bytes();
     const size_t budget = probe_smem_budget(info);
-    const size_t stage = (size_t)pl.outcap * 2 * PB;
-    uint32_t cap = 64;
-    while ((size_t)(cap * 2) * slot + stage <= budget && cap < 16384) cap <<= 1;
-    pl.rcap = cap / 2;
+    // largest table (then largest probe sub-chunk) whose probe block fits two per SM
+    bool found = false;
+    for (uint32_t sub = 1024; sub >= 256 && !found; sub >>= 1) {
+        for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
+            const uint32_t outcap = sub + sub / 2;
+            if (ProbeSmem<KW, PB, HS>::bytes(rcap, 2 * rcap, sub, outcap) <= budget && (rcap >= 1024 || sub == 256)) {
+                pl.rcap = rcap;
+                pl.sub = sub;
+                pl.outcap = outcap;
+                found = true;
+                break;
+            }
+        }
+    }
     if (opt && opt->build_rows > 0) {
         uint32_t want = 32;
         while (want < (uint32_t)opt->build_rows && want < pl.rcap) want <<= 1;
@@ -70,6 +80,10 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     }
     if (opt && opt->probe_rows > 0) {
         pl.schunk = (uint32_t)opt->probe_rows;
+        if (pl.sub > pl.schunk) {
+            pl.sub = pl.schunk < 32 ? 32 : pl.schunk;
+            pl.outcap = pl.sub + pl.sub / 2;
+        }
     }
     // passes / bits: the average build partition should fill about half a table
     int total_bits = 0;
@@ -118,7 +132,6 @@ int ensure_smem(K kernel, size_t bytes) {
     return VJ_OK;
 }
 
-constexpr int SCATTER_ITEMS = 8;
 
 struct PassBufs {
     uint4 *units;
@@ -164,9 +177,10 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
     unit_scan_kernel<<<bins, PLAN_THREADS, us_smem, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCAN_END + 4 * pass, stream);
-    const size_t sc_smem = ScatterSmem<KW, PB, HS, SCATTER_ITEMS>::bytes(bins);
-    VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, SCATTER_ITEMS>, sc_smem));
-    scatter_kernel<KW, PB, HS, SCATTER_ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
+    constexpr int ITEMS = scatter_items<KW, PB, HS>();
+    const size_t sc_smem = ScatterSmem<KW, PB, HS, ITEMS>::bytes(bins);
+    VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, ITEMS>, sc_smem));
+    scatter_kernel<KW, PB, HS, ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCATTER_END + 4 * pass, stream);
     if (ctx) ctx->launches += 5;
@@ -209,28 +223,30 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     const int np = pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1);
 
     // ---- workspace layout (dry run, then carve)
-    auto layout = [&](Carver &c, void **bufA, void **bufB, PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
+    const uint64_t item_cap = (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    auto layout = [&](Carver &c, void **bufA, void **bufB, PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **item_part, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
         const size_t table_bytes = ((size_t)in.rows[0] + in.rows[1]) * row_bytes + 4 * 256;
         *bufA = pl.passes >= 1 ? c.take<char>(table_bytes) : nullptr;
         *bufB = pl.passes >= 2 ? c.take<char>(table_bytes) : nullptr;
         if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, pl.max_units[0]);
         if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, pl.max_units[1]);
-        *item_begin = c.take<uint32_t>((size_t)np + 1);
+        *item_begin = c.take<uint32_t>((size_t)np + 2);
+        *item_part = c.take<uint32_t>(item_cap);
         *ticket = c.take<uint32_t>(1);
         *out_count = c.take<unsigned long long>(1);
         *error = c.take<uint32_t>(1);
     };
     void *bufA, *bufB;
     PassBufs pb0{}, pb1{};
-    uint32_t *item_begin, *ticket, *error;
+    uint32_t *item_begin, *item_part, *ticket, *error;
     unsigned long long *out_count;
     Carver dry;
-    layout(dry, &bufA, &bufB, &pb0, &pb1, &item_begin, &ticket, &out_count, &error);
+    layout(dry, &bufA, &bufB, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
     void *ws = nullptr;
     VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
     Carver c;
     c.base = (char *)ws;
-    layout(c, &bufA, &bufB, &pb0, &pb1, &item_begin, &ticket, &out_count, &error);
+    layout(c, &bufA, &bufB, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
     VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
     ctx->launches = 0;
 
@@ -275,6 +291,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         P.hs = hs;
         P.max_units = pl.max_units[pass];
         P.min_unit_rows = 4096;
+        P.error = error;
         const PassBufs &pb = pass == 0 ? pb0 : pb1;
         VJ_TRY((run_pass<KW, PB, HS>(ctx, pass, P, pb, stream)));
         for (int s = 0; s < 2; s++) {
@@ -308,7 +325,10 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.rcap = pl.rcap;
     Pq.schunk = pl.schunk;
     Pq.outcap = pl.outcap;
+    Pq.sub_rows = pl.sub;
     Pq.item_begin = item_begin;
+    Pq.item_part = item_part;
+    Pq.item_cap = (uint32_t)(item_cap < 0xffffffffull ? item_cap : 0xffffffffull);
     Pq.ticket = ticket;
     Pq.out_count = out_count;
     Pq.hs = hs;
@@ -316,7 +336,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     run->probe = Pq;
     run->d_out_count = out_count;
     run->d_error = error;
-    run->probe_smem = ProbeSmem<KW, PB, HS>::bytes(2 * pl.rcap, pl.outcap);
+    run->probe_smem = ProbeSmem<KW, PB, HS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
     VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS>, run->probe_smem));
     VJ_TRY((probe_grid<KW, PB, HS>(ctx->info, run->probe_smem, &run->probe_grid)));
     return VJ_OK;
@@ -450,20 +470,23 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     const int bins = 1 << bits;
     const int G = 1;
     const int max_units = ctx->info.sms * 16 + G;
-    auto layout = [&](Carver &c, PassBufs *pb, unsigned long long **hist, unsigned long long **off) {
+    auto layout = [&](Carver &c, PassBufs *pb, unsigned long long **hist, unsigned long long **off, uint32_t **err) {
         *pb = carve_pass(c, G, bins, max_units);
         *hist = c.take<unsigned long long>(bins);
         *off = c.take<unsigned long long>(bins);
+        *err = c.take<uint32_t>(1);
     };
     PassBufs pb;
     unsigned long long *dh, *doff;
+    uint32_t *derr;
     Carver dry;
-    layout(dry, &pb, &dh, &doff);
+    layout(dry, &pb, &dh, &doff, &derr);
     void *ws = nullptr;
     VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
     Carver c;
     c.base = (char *)ws;
-    layout(c, &pb, &dh, &doff);
+    layout(c, &pb, &dh, &doff, &derr);
+    VJ_CUDA(cudaMemsetAsync(derr, 0, sizeof(uint32_t), stream));
     PassParams P{};
     P.side[0].keys_in = in->keys;
     P.side[0].pay_in = in->payloads;
@@ -480,6 +503,7 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     P.hs = hs;
     P.max_units = max_units;
     P.min_unit_rows = 4096;
+    P.error = derr;
     if (in->rows > 0) {
         VJ_TRY((run_pass<KW, PB, HS>(ctx, 0, P, pb, stream)));
     } else {
@@ -491,7 +515,10 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     if (h_hist || h_off) {
         if (h_hist) VJ_CUDA(cudaMemcpyAsync(h_hist, d_hist ? (void *)d_hist : (void *)dh, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
         if (h_off) VJ_CUDA(cudaMemcpyAsync(h_off, d_off ? (void *)d_off : (void *)doff, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+        uint32_t herr = 0;
+        VJ_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         VJ_CUDA(cudaStreamSynchronize(stream));
+        VJ_CHECK(herr == 0, VJ_ERR_DEVICE, "vj_partition: a kernel reported an internal limit (flags %x)", herr);
     }
     return VJ_OK;
 }
@@ -720,14 +747,15 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     cudaStream_t st = (cudaStream_t)stream;
     *count = 0;
     const size_t kb = (size_t)r->key_words * 4, pb = (size_t)r->payload_bytes;
-    const size_t need = (r->rows + s->rows) * (kb + pb) + 4 * 256;
+    // one cached device buffer holds both tables and the output pairs
+    const size_t need = (r->rows + s->rows) * (kb + pb) + (size_t)capacity * 2 * pb + 6 * 256;
     if (ctx->stage_bytes < need) {
         if (ctx->stage) {
             VJ_CUDA(cudaFreeAsync(ctx->stage, st));
             ctx->stage = nullptr;
             ctx->stage_bytes = 0;
         }
-        VJ_CHECK(!ctx->budget || ctx->owned_bytes + ctx->workspace_bytes + need <= ctx->budget, VJ_ERR_BUDGET, "vj_join_host: input staging exceeds the context budget");
+        VJ_CHECK(!ctx->budget || ctx->owned_bytes + ctx->workspace_bytes + need <= ctx->budget, VJ_ERR_BUDGET, "vj_join_host: staging exceeds the context budget");
         VJ_CUDA(cudaMallocAsync(&ctx->stage, need, st));
         ctx->stage_bytes = need;
     }
@@ -735,6 +763,7 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     c.base = (char *)ctx->stage;
     void *rk = c.take<char>(r->rows * kb), *rp = c.take<char>(r->rows * pb);
     void *sk = c.take<char>(s->rows * kb), *sp = c.take<char>(s->rows * pb);
+    void *dpairs = c.take<char>((size_t)capacity * 2 * pb);
     if (r->rows) {
         VJ_CUDA(cudaMemcpyAsync(rk, r->keys, r->rows * kb, cudaMemcpyHostToDevice, st));
         VJ_CUDA(cudaMemcpyAsync(rp, r->payloads, r->rows * pb, cudaMemcpyHostToDevice, st));
@@ -749,9 +778,18 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     ds.keys = sk;
     ds.payloads = sp;
     vj_result res{};
-    VJ_TRY(vj_join(ctx, &dr, &ds, options, &res, stream));
+    if (capacity > 0) {
+        res.pairs = dpairs;
+        res.capacity = capacity;
+    } else {
+        res.pairs = nullptr;  // count only: library-owned buffer, never copied back
+    }
+    int status = vj_join(ctx, &dr, &ds, options, &res, stream);
     *count = res.count;
-    int status = VJ_OK;
+    if (status == VJ_ERR_CAPACITY) {
+        return status;
+    }
+    VJ_TRY(status);
     if (res.count > capacity) {
         status = set_error(VJ_ERR_CAPACITY, "vj_join_host: %llu pairs, capacity %llu", (unsigned long long)res.count, (unsigned long long)capacity);
     } else if (res.count) {
@@ -760,6 +798,8 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) status = cuda_error(e, "vj_join_host: copy of pairs to the host");
     }
-    vj_result_free(ctx, &res);
+    if (res.owned) {
+        vj_result_free(ctx, &res);
+    }
     return status;
 }

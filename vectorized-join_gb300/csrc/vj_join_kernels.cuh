@@ -65,6 +65,7 @@ struct PassParams {
     uint32_t *unit_off;          // [max_units][bins]
     uint32_t *part_begin;        // [G*bins]
     uint32_t *part_end;          // [G*bins]
+    uint32_t *error;             // bit 4: a bulk-copy wait ran out
 };
 
 struct ProbeParams {
@@ -77,7 +78,10 @@ struct ProbeParams {
     uint32_t rcap;     // build rows per item (table capacity = 2*rcap rounded up to pow2)
     uint32_t schunk;   // probe rows per item
     uint32_t outcap;   // staged output pairs per block
-    uint32_t *item_begin;  // [np+1]
+    uint32_t *item_begin;  // [np+2]: prefix, total, and whether item_part is filled
+    uint32_t *item_part;   // [item_cap]: partition of each item
+    uint32_t item_cap;
+    uint32_t sub_rows;     // probe rows per bulk copy
     uint32_t *ticket;
     unsigned long long *out_count;
     void *out;
@@ -341,30 +345,70 @@ __global__ void __launch_bounds__(PLAN_THREADS) unit_scan_kernel(PassParams P) {
     }
 }
 
+// Shared memory of the scatter kernel: two input tiles filled by bulk copies (each column
+// as its 16-byte aligned window), the bucket-sorted output tile, bucket ids and counters.
 template <int KW, int PB, int HS, int ITEMS>
 struct ScatterSmem {
-    using P = typename PayloadType<PB>::T;
     static constexpr int T = PART_THREADS * ITEMS;
-    static size_t bytes(uint32_t bins) {
-        return (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2) + (size_t)bins * 3 * 4;
-    }
+    static constexpr size_t col(size_t bytes) { return (bytes + 32 + 15) / 16 * 16; }
+    static constexpr size_t KEYS = col((size_t)T * KW * 4);
+    static constexpr size_t PAY = col((size_t)T * PB);
+    static constexpr size_t HASH = HS ? col((size_t)T * HS) : 0;
+    static constexpr size_t IN_BUF = KEYS + PAY + HASH;
+    static constexpr size_t OUT = (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2);
+    static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 3 * 4; }
 };
+
+// Rows per thread of a scatter tile: the largest of 8, 4, 2 whose block (with 2^10 bins)
+// stays within about half of an SM's shared memory, so two blocks fit per SM (wider
+// passes, up to 2^12 bins, stay below the 227 KB block limit with one block per SM).
+template <int KW, int PB, int HS>
+constexpr int scatter_items() {
+    return ScatterSmem<KW, PB, HS, 8>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, 8>::OUT + 16 + 1024 * 12 <= 113 * 1024   ? 8
+           : ScatterSmem<KW, PB, HS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, 4>::OUT + 16 + 1024 * 12 <= 113 * 1024 ? 4
+                                                                                                                     : 2;
+}
+
+// One tile of a unit: rows [a, b) of one side, copied column by column into input buffer
+// `buf` (issued by one thread).
+template <int KW, int PB, int HS, int ITEMS>
+__device__ __forceinline__ void scatter_issue(const Side &S, uint32_t a, uint32_t b, unsigned char *inb, uint64_t *bar, uint32_t *delta) {
+    using SM = ScatterSmem<KW, PB, HS, ITEMS>;
+    const ColWindow wk = col_window(S.keys_in, KW * 4, a, b);
+    const ColWindow wp = col_window(S.pay_in, PB, a, b);
+    uint32_t total = wk.bytes + wp.bytes;
+    ColWindow wh{nullptr, 0, 0};
+    if (HS) {
+        wh = col_window(S.hash_in, HS, a, b);
+        total += wh.bytes;
+    }
+    delta[0] = wk.delta;
+    delta[1] = wp.delta;
+    delta[2] = wh.delta;
+    mbar_arrive_expect_tx(bar, total);
+    bulk_g2s(inb, wk.src, wk.bytes, bar);
+    bulk_g2s(inb + SM::KEYS, wp.src, wp.bytes, bar);
+    if (HS) bulk_g2s(inb + SM::KEYS + SM::PAY, wh.src, wh.bytes, bar);
+}
 
 template <int KW, int PB, int HS, int ITEMS>
 __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     using Pt = typename PayloadType<PB>::T;
-    constexpr int T = PART_THREADS * ITEMS;
+    using SM = ScatterSmem<KW, PB, HS, ITEMS>;
+    constexpr int T = SM::T;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    // staging layout: keys | payloads | hashes | bucket ids | run | cnt | start
-    Key<KW> *st_key = (Key<KW> *)s_raw;
-    Pt *st_pay = (Pt *)(s_raw + (size_t)T * KW * 4);
-    unsigned long long *st_hash = (unsigned long long *)(s_raw + (size_t)T * (KW * 4 + PB));
-    uint16_t *st_b = (uint16_t *)(s_raw + (size_t)T * (KW * 4 + PB + (HS ? 8 : 0)));
+    uint64_t *bar = (uint64_t *)s_raw;
+    unsigned char *inb0 = s_raw + 16;
+    unsigned char *out_keys = inb0 + 2 * SM::IN_BUF;
+    Pt *out_pay = (Pt *)(out_keys + (size_t)T * KW * 4);
+    unsigned long long *out_hash = (unsigned long long *)((unsigned char *)out_pay + (size_t)T * PB);
+    uint16_t *st_b = (uint16_t *)((unsigned char *)out_hash + (HS ? (size_t)T * 8 : 0));
     const uint32_t bins = 1u << P.bits;
-    uint32_t *s_run = (uint32_t *)(s_raw + (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2));
+    uint32_t *s_run = (uint32_t *)(st_b + T);
     uint32_t *s_cnt = s_run + bins;
     uint32_t *s_start = s_cnt + bins;
     __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_delta[2][3];
 
     const uint32_t u = blockIdx.x;
     if (u >= *P.unit_count) return;
@@ -373,26 +417,48 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     const uint64_t mask = bins - 1;
     const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
     const uint32_t b0 = threadIdx.x * per;
+    const uint32_t ntiles = (U.z - U.y + T - 1) / T;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_proxy_async();
+    }
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_run[b] = P.unit_off[(size_t)u * bins + b];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t k = 0; k < 2 && k < ntiles; k++) {
+            const uint32_t a = U.y + k * T;
+            scatter_issue<KW, PB, HS, ITEMS>(S, a, min(U.z, a + T), inb0 + k * SM::IN_BUF, &bar[k], s_delta[k]);
+        }
+    }
 
-    for (uint32_t tile = U.y; tile < U.z; tile += T) {
-        const uint32_t nt = U.z - tile < (uint32_t)T ? U.z - tile : (uint32_t)T;
+    for (uint32_t k = 0; k < ntiles; k++) {
+        const uint32_t buf = k & 1;
+        const uint32_t tile = U.y + k * T;
+        const uint32_t nt = min(U.z - tile, (uint32_t)T);
         for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_cnt[b] = 0;
-        __syncthreads();
-        Row<KW, PB, HS> row[ITEMS];
+        const bool ok = mbar_wait(&bar[buf], (k >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicOr(P.error, 4u);
+            // let any other copy of this block land before leaving
+            if (k + 1 < ntiles) mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
+            return;
+        }
+        const unsigned char *kc = inb0 + buf * SM::IN_BUF + s_delta[buf][0];
+        const Pt *pc = (const Pt *)(inb0 + buf * SM::IN_BUF + SM::KEYS + s_delta[buf][1]);
+        const unsigned char *hc = inb0 + buf * SM::IN_BUF + SM::KEYS + SM::PAY + s_delta[buf][2];
         uint32_t bk[ITEMS];
         uint32_t rk[ITEMS];
 #pragma unroll
-        for (int k = 0; k < ITEMS; k++) {
-            const uint32_t i = k * PART_THREADS + threadIdx.x;
-            if (i < nt) load_row<KW, PB, HS>(S.keys_in, S.pay_in, S.hash_in, tile + i, P.hs, row[k]);
-        }
-#pragma unroll
-        for (int k = 0; k < ITEMS; k++) {
-            const uint32_t i = k * PART_THREADS + threadIdx.x;
+        for (int j = 0; j < ITEMS; j++) {
+            const uint32_t i = j * PART_THREADS + threadIdx.x;
             if (i < nt) {
-                bk[k] = (uint32_t)((bucket_hash(row[k].h, P.hs) >> P.shift) & mask);
-                rk[k] = atomicAdd(&s_cnt[bk[k]], 1u);
+                uint64_t h;
+                if (HS == 8) h = ((const unsigned long long *)hc)[i];
+                else if (HS == 4) h = ((const uint32_t *)hc)[i];
+                else h = row_hash<KW>(key_from_smem<KW>(kc + (size_t)i * KW * 4), P.hs);
+                bk[j] = (uint32_t)((bucket_hash(h, P.hs) >> P.shift) & mask);
+                rk[j] = atomicAdd(&s_cnt[bk[j]], 1u);
             }
         }
         __syncthreads();
@@ -407,25 +473,31 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < ITEMS; k++) {
-            const uint32_t i = k * PART_THREADS + threadIdx.x;
+        for (int j = 0; j < ITEMS; j++) {
+            const uint32_t i = j * PART_THREADS + threadIdx.x;
             if (i < nt) {
-                const uint32_t pos = s_start[bk[k]] + rk[k];
-                st_key[pos] = row[k].k;
-                st_pay[pos] = row[k].p;
-                if (HS) st_hash[pos] = row[k].h;
-                st_b[pos] = (uint16_t)bk[k];
+                const uint32_t pos = s_start[bk[j]] + rk[j];
+                key_to_smem<KW>(out_keys + (size_t)pos * KW * 4, key_from_smem<KW>(kc + (size_t)i * KW * 4));
+                out_pay[pos] = pc[i];
+                if (HS == 8) out_hash[pos] = ((const unsigned long long *)hc)[i];
+                else if (HS == 4) out_hash[pos] = ((const uint32_t *)hc)[i];
+                st_b[pos] = (uint16_t)bk[j];
             }
         }
-        __syncthreads();
+        __syncthreads();  // input buffer `buf` is free: refill it with tile k + 2
+        if (threadIdx.x == 0 && k + 2 < ntiles) {
+            fence_proxy_async();
+            const uint32_t a = U.y + (k + 2) * T;
+            scatter_issue<KW, PB, HS, ITEMS>(S, a, min(U.z, a + T), inb0 + buf * SM::IN_BUF, &bar[buf], s_delta[buf]);
+        }
         for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
             const uint32_t b = st_b[i];
             const uint32_t dst = s_run[b] + i - s_start[b];
-            store_key<KW>(S.keys_out, dst, st_key[i]);
-            __stcs((Pt *)S.pay_out + dst, st_pay[i]);
+            store_key<KW>(S.keys_out, dst, key_from_smem<KW>(out_keys + (size_t)i * KW * 4));
+            ((Pt *)S.pay_out)[dst] = out_pay[i];
             if (HS && S.hash_out) {
-                if (HS == 8) ((unsigned long long *)S.hash_out)[dst] = st_hash[i];
-                else ((uint32_t *)S.hash_out)[dst] = (uint32_t)st_hash[i];
+                if (HS == 8) ((unsigned long long *)S.hash_out)[dst] = out_hash[i];
+                else ((uint32_t *)S.hash_out)[dst] = (uint32_t)out_hash[i];
             }
         }
         __syncthreads();
@@ -444,9 +516,9 @@ __device__ __forceinline__ unsigned long long items_of(const ProbeParams &Q, int
     return (unsigned long long)((nr + Q.rcap - 1) / Q.rcap) * ((ns + Q.schunk - 1) / Q.schunk);
 }
 
-// One block. Work items per partition and their prefix; resets the ticket and counter.
-// A plan of 2^31 or more items (only reachable when almost every row shares one hash)
-// is refused with error flag 2 and no items.
+// One block. Work items per partition, their prefix and the partition of every item;
+// resets the ticket and counter. A plan of 2^31 or more items (only reachable when almost
+// every row shares one hash) is refused with error flag 2 and no items.
 __global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q) {
     __shared__ unsigned long long s_warp[32];
     const int per = (Q.np + PLAN_THREADS - 1) / PLAN_THREADS;
@@ -456,12 +528,18 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q)
     unsigned long long total = 0;
     unsigned long long run = block_exclusive_scan<unsigned long long>(mine, s_warp, &total);
     const bool too_many = total >= (1ull << 31);
+    const bool fill = !too_many && total <= Q.item_cap;
     for (int p = p0; p < p0 + per && p < Q.np; p++) {
         Q.item_begin[p] = too_many ? 0u : (uint32_t)run;
-        run += items_of(Q, p);
+        const unsigned long long n = items_of(Q, p);
+        if (fill) {
+            for (unsigned long long k = 0; k < n; k++) Q.item_part[run + k] = (uint32_t)p;
+        }
+        run += n;
     }
     if (threadIdx.x == 0) {
         Q.item_begin[Q.np] = too_many ? 0u : (uint32_t)total;
+        Q.item_begin[Q.np + 1] = fill ? 1u : 0u;
         if (too_many) atomicOr(Q.error, 2u);
         *Q.ticket = 0;
         *Q.out_count = 0;
@@ -481,11 +559,65 @@ struct Pair<8> {
     static __device__ __forceinline__ T make(unsigned long long a, unsigned long long b) { return make_ulonglong2(a, b); }
 };
 
+// Shared memory of the probe kernel: the build chunk as copied (each column as its
+// 16-byte aligned window), the open-addressing table of build-row indices, two probe
+// sub-chunks filled by bulk copies, and the output staging area.
 template <int KW, int PB, int HS>
 struct ProbeSmem {
-    static size_t slot_bytes() { return 4 + KW * 4 + PB + (HS ? 8 : 0); }
-    static size_t bytes(uint32_t cap, uint32_t outcap) { return (size_t)cap * slot_bytes() + (size_t)outcap * 2 * PB; }
+    __host__ __device__ static size_t col(size_t bytes) { return (bytes + 32 + 15) / 16 * 16; }
+    __host__ __device__ static size_t rows_bytes(uint32_t rows) { return col((size_t)rows * KW * 4) + col((size_t)rows * PB) + (HS ? col((size_t)rows * HS) : 0); }
+    __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t sub, uint32_t outcap) {
+        return 32 + rows_bytes(rcap) + (size_t)tcap * 4 + 2 * rows_bytes(sub) + (size_t)outcap * 2 * PB;
+    }
 };
+
+// Column views of a chunk copied into shared memory.
+template <int KW, int PB, int HS>
+struct SmemRows {
+    const unsigned char *keys;
+    const typename PayloadType<PB>::T *pay;
+    const unsigned char *hash;
+    __device__ __forceinline__ Key<KW> key(uint32_t i) const { return key_from_smem<KW>(keys + (size_t)i * KW * 4); }
+    __device__ __forceinline__ uint64_t h(uint32_t i, const HashSpec &hs) const {
+        if (HS == 8) return ((const unsigned long long *)hash)[i];
+        if (HS == 4) return ((const uint32_t *)hash)[i];
+        return row_hash<KW>(key(i), hs);
+    }
+};
+
+// Issue the copies of rows [a, b) of one table into `dst` (sized for `cap` rows); the
+// returned views are valid once `bar` completes.
+template <int KW, int PB, int HS>
+__device__ __forceinline__ void probe_issue(const void *keys, const void *pay, const void *hash, uint32_t a, uint32_t b, uint32_t cap, unsigned char *dst, uint64_t *bar, uint32_t *delta) {
+    using SM = ProbeSmem<KW, PB, HS>;
+    const ColWindow wk = col_window(keys, KW * 4, a, b);
+    const ColWindow wp = col_window(pay, PB, a, b);
+    uint32_t total = wk.bytes + wp.bytes;
+    ColWindow wh{nullptr, 0, 0};
+    if (HS) {
+        wh = col_window(hash, HS, a, b);
+        total += wh.bytes;
+    }
+    delta[0] = wk.delta;
+    delta[1] = wp.delta;
+    delta[2] = wh.delta;
+    const size_t kcol = SM::col((size_t)cap * KW * 4), pcol = SM::col((size_t)cap * PB);
+    mbar_arrive_expect_tx(bar, total);
+    bulk_g2s(dst, wk.src, wk.bytes, bar);
+    bulk_g2s(dst + kcol, wp.src, wp.bytes, bar);
+    if (HS) bulk_g2s(dst + kcol + pcol, wh.src, wh.bytes, bar);
+}
+
+template <int KW, int PB, int HS>
+__device__ __forceinline__ SmemRows<KW, PB, HS> rows_view(const unsigned char *buf, uint32_t cap, const uint32_t *delta) {
+    using SM = ProbeSmem<KW, PB, HS>;
+    const size_t kcol = SM::col((size_t)cap * KW * 4), pcol = SM::col((size_t)cap * PB);
+    SmemRows<KW, PB, HS> v;
+    v.keys = buf + delta[0];
+    v.pay = (const typename PayloadType<PB>::T *)(buf + kcol + delta[1]);
+    v.hash = buf + kcol + pcol + delta[2];
+    return v;
+}
 
 // Write the staged pairs [0, n) to the output at a block of positions taken from the
 // global counter; positions at or past the capacity are dropped (the count still grows).
@@ -505,56 +637,93 @@ template <int KW, int PB, int HS>
 __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
     using Pt = typename PayloadType<PB>::T;
     using PT = typename Pair<PB>::T;
+    using SM = ProbeSmem<KW, PB, HS>;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    const uint32_t max_cap = 2 * Q.rcap;  // rcap is a power of two
-    // layout: pairs staging | payloads | keys | hashes | slot index
-    PT *stage = (PT *)s_raw;
-    Pt *t_pay = (Pt *)(s_raw + (size_t)Q.outcap * sizeof(PT));
-    Key<KW> *t_key = (Key<KW> *)((unsigned char *)t_pay + (size_t)max_cap * PB);
-    unsigned long long *t_hash = (unsigned long long *)((unsigned char *)t_key + (size_t)max_cap * KW * 4);
-    uint32_t *t_idx = (uint32_t *)((unsigned char *)t_hash + (HS ? (size_t)max_cap * 8 : 0));
+    const uint32_t tcap_max = 2 * Q.rcap;  // rcap is a power of two
+    // layout: barriers | build chunk | table | probe sub-chunks x2 | output staging
+    uint64_t *bar = (uint64_t *)s_raw;     // [0] build chunk, [1], [2] probe sub-chunks
+    unsigned char *rbuf = s_raw + 32;
+    uint32_t *t_idx = (uint32_t *)(rbuf + SM::rows_bytes(Q.rcap));
+    unsigned char *sbuf0 = (unsigned char *)(t_idx + tcap_max);
+    const size_t sbytes = SM::rows_bytes(Q.sub_rows);
+    PT *stage = (PT *)(sbuf0 + 2 * sbytes);
 
-    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_item, s_part;
     __shared__ uint32_t s_out_n;
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_rdelta[3];
+    __shared__ uint32_t s_sdelta[2][3];
     const int lane = threadIdx.x & 31;
     const uint32_t total_items = Q.item_begin[Q.np];
-    if (threadIdx.x == 0) s_out_n = 0;
+    const bool direct = Q.item_begin[Q.np + 1] != 0;
+    if (threadIdx.x == 0) {
+        s_out_n = 0;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
+        fence_proxy_async();
+    }
+    uint32_t r_loads = 0;   // build-chunk copies waited for so far (parity of bar[0])
+    uint32_t s_issued = 0;  // probe sub-chunk copies issued / waited for
+    uint32_t s_waited = 0;
 
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) s_item = atomicAdd(Q.ticket, 1u);
+        if (threadIdx.x == 0) {
+            const uint32_t it = atomicAdd(Q.ticket, 1u);
+            uint32_t p = 0;
+            if (it < total_items) {
+                if (direct) {
+                    p = Q.item_part[it];
+                } else {
+                    int lo = 0, hi = Q.np - 1;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (Q.item_begin[mid] <= it) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    p = (uint32_t)lo;
+                }
+            }
+            s_item = it;
+            s_part = p;
+        }
         __syncthreads();
         const uint32_t item = s_item;
         if (item >= total_items) break;
-        // partition of this item: last p with item_begin[p] <= item
-        int lo = 0, hi = Q.np - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (Q.item_begin[mid] <= item) lo = mid;
-            else hi = mid - 1;
-        }
-        const int p = lo;
+        const uint32_t p = s_part;
         const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
         const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
         const uint32_t nsc = (se - sb + Q.schunk - 1) / Q.schunk;
         const uint32_t k = item - Q.item_begin[p];
         const uint32_t r0 = rb + (k / nsc) * Q.rcap;
-        const uint32_t r1 = re - r0 < Q.rcap ? re : r0 + Q.rcap;
+        const uint32_t r1 = min(re, r0 + Q.rcap);
         const uint32_t s0 = sb + (k % nsc) * Q.schunk;
-        const uint32_t s1 = se - s0 < Q.schunk ? se : s0 + Q.schunk;
+        const uint32_t s1 = min(se, s0 + Q.schunk);
         const uint32_t nr = r1 - r0;
+        const uint32_t nsub = (s1 - s0 + Q.sub_rows - 1) / Q.sub_rows;
         uint32_t cap = 64;
-        while (cap < 2 * nr) cap <<= 1;
+        while (cap < 4 * nr && cap < tcap_max) cap <<= 1;
         const uint32_t cmask = cap - 1;
 
-        // ---- build
+        if (threadIdx.x == 0) {
+            probe_issue<KW, PB, HS>(Q.r_keys, Q.r_pay, Q.r_hash, r0, r1, Q.rcap, rbuf, &bar[0], s_rdelta);
+            const uint32_t sbi = s_issued & 1;
+            probe_issue<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, s0, min(s1, s0 + Q.sub_rows), Q.sub_rows, sbuf0 + sbi * sbytes, &bar[1 + sbi], s_sdelta[sbi]);
+        }
+        s_issued++;
         for (uint32_t i = threadIdx.x; i < cap; i += PROBE_THREADS) t_idx[i] = 0;
-        __syncthreads();
+        bool ok = mbar_wait(&bar[0], r_loads & 1);
+        r_loads++;
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicOr(Q.error, 4u);
+            mbar_wait(&bar[1 + ((s_issued - 1) & 1)], ((s_issued - 1) >> 1) & 1);
+            return;
+        }
+        // ---- build: table of build-row indices (+1) keyed by the mixed hash
+        const SmemRows<KW, PB, HS> R = rows_view<KW, PB, HS>(rbuf, Q.rcap, s_rdelta);
         for (uint32_t i = threadIdx.x; i < nr; i += PROBE_THREADS) {
-            Row<KW, PB, HS> r;
-            load_row<KW, PB, HS>(Q.r_keys, Q.r_pay, Q.r_hash, r0 + i, Q.hs, r);
-            uint32_t slot = (uint32_t)fmix64(r.h) & cmask;
+            uint32_t slot = (uint32_t)fmix64(R.h(i, Q.hs)) & cmask;
             uint32_t tries = 0;
             while (atomicCAS(&t_idx[slot], 0u, i + 1) != 0u) {
                 slot = (slot + 1) & cmask;
@@ -563,37 +732,54 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                     break;
                 }
             }
-            t_key[slot] = r.k;
-            t_pay[slot] = r.p;
-            if (HS) t_hash[slot] = r.h;
         }
         __syncthreads();
 
-        // ---- probe
-        for (uint32_t base = s0; base < s1; base += PROBE_THREADS * PROBE_ITEMS) {
-            Row<KW, PB, HS> srow[PROBE_ITEMS];
-#pragma unroll
-            for (int j = 0; j < PROBE_ITEMS; j++) {
-                const uint32_t i = base + j * PROBE_THREADS + threadIdx.x;
-                if (i < s1) load_row<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, i, Q.hs, srow[j]);
+        // ---- probe the sub-chunks of this item, the next one loading meanwhile
+        for (uint32_t sub = 0; sub < nsub; sub++) {
+            const uint32_t sbi = s_waited & 1;
+            ok = mbar_wait(&bar[1 + sbi], (s_waited >> 1) & 1);
+            s_waited++;
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicOr(Q.error, 4u);
+                return;
             }
-#pragma unroll
-            for (int j = 0; j < PROBE_ITEMS; j++) {
-                const uint32_t i = base + j * PROBE_THREADS + threadIdx.x;
-                bool active = i < s1;
-                uint32_t slot = active ? (uint32_t)fmix64(srow[j].h) & cmask : 0;
+            if (sub + 1 < nsub) {
+                if (threadIdx.x == 0) {
+                    fence_proxy_async();
+                    const uint32_t a = s0 + (sub + 1) * Q.sub_rows;
+                    const uint32_t nbi = s_issued & 1;
+                    probe_issue<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, a, min(s1, a + Q.sub_rows), Q.sub_rows, sbuf0 + nbi * sbytes, &bar[1 + nbi], s_sdelta[nbi]);
+                }
+                s_issued++;
+            }
+            const SmemRows<KW, PB, HS> Sv = rows_view<KW, PB, HS>(sbuf0 + sbi * sbytes, Q.sub_rows, s_sdelta[sbi]);
+            const uint32_t a = s0 + sub * Q.sub_rows;
+            const uint32_t ns = min(s1 - a, Q.sub_rows);
+            for (uint32_t base = 0; base < ns; base += PROBE_THREADS) {
+                const uint32_t i = base + threadIdx.x;
+                bool active = i < ns;
+                Key<KW> skey;
+                uint64_t sh = 0;
+                uint32_t slot = 0;
+                if (active) {
+                    skey = Sv.key(i);
+                    sh = Sv.h(i, Q.hs);
+                    slot = (uint32_t)fmix64(sh) & cmask;
+                }
                 // Lanes walk their probe sequences in lock step; each step emits the lanes
                 // that matched with one shared-memory reservation per warp.
                 while (__any_sync(0xffffffffu, active)) {
                     bool match = false;
                     Pt rp = 0;
                     if (active) {
-                        if (t_idx[slot] == 0) {
+                        const uint32_t e = t_idx[slot];
+                        if (e == 0) {
                             active = false;
                         } else {
-                            if (key_equal<KW>(t_key[slot], srow[j].k) && (!HS || t_hash[slot] == srow[j].h)) {
+                            if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.h(e - 1, Q.hs) == sh)) {
                                 match = true;
-                                rp = t_pay[slot];
+                                rp = R.pay[e - 1];
                             }
                             slot = (slot + 1) & cmask;
                         }
@@ -606,12 +792,13 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                         pos0 = __shfl_sync(0xffffffffu, pos0, leader);
                         if (match) {
                             const uint32_t pos = pos0 + __popc(m & lanemask_lt());
+                            const Pt sp = Sv.pay[i];
                             if (pos < Q.outcap) {
-                                stage[pos] = Pair<PB>::make(rp, srow[j].p);
+                                stage[pos] = Pair<PB>::make(rp, sp);
                             } else {
                                 // staging full (build rows with many duplicates): direct write
-                                unsigned long long g = atomicAdd(Q.out_count, 1ull);
-                                if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, srow[j].p);
+                                const unsigned long long g = atomicAdd(Q.out_count, 1ull);
+                                if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, sp);
                             }
                         }
                     }
@@ -620,10 +807,11 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
             __syncthreads();
             uint32_t n = s_out_n;
             if (n > Q.outcap) n = Q.outcap;
-            if (n + PROBE_THREADS * PROBE_ITEMS > Q.outcap) {
+            if (n + Q.sub_rows > Q.outcap) {
                 flush_pairs<PB>(Q, stage, n, &s_base);
                 __syncthreads();
                 if (threadIdx.x == 0) s_out_n = 0;
+                __syncthreads();
             }
         }
     }

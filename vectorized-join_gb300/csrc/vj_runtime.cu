@@ -317,6 +317,14 @@ extern "C" int vj_ctx_create(int device, uint64_t memory_budget_bytes, vj_ctx **
     VJ_CUDA(cudaGetDeviceCount(&count));
     VJ_CHECK(device >= 0 && device < count, VJ_ERR_INVALID_ARGUMENT, "vj_ctx_create: device %d of %d", device, count);
     VJ_CUDA(cudaSetDevice(device));
+    // Keep freed stream-ordered memory in the device's default pool instead of unmapping it
+    // at every synchronisation, so repeated joins do not remap their workspace. This is a
+    // property of this process's pool, not of the GPU.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     vj_ctx *c = new vj_ctx();
     c->device = device;
     c->budget = memory_budget_bytes;
