@@ -64,7 +64,8 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     for (uint32_t sub = 1024; sub >= 256 && !found; sub >>= 1) {
         for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
             const uint32_t outcap = sub + sub / 2;
-            if (ProbeSmem<KW, PB, HS>::bytes(rcap, 2 * rcap, sub, outcap) <= budget && (rcap >= 1024 || sub == 256)) {
+            // sized for row-contiguous chunks, which are never smaller than columnar ones
+            if (ProbeSmem<KW, PB, HS, true>::bytes(rcap, 2 * rcap, sub, outcap) <= budget && (rcap >= 1024 || sub == 256)) {
                 pl.rcap = rcap;
                 pl.sub = sub;
                 pl.outcap = outcap;
@@ -151,7 +152,7 @@ PassBufs carve_pass(Carver &c, int G, int bins, int max_units) {
     return b;
 }
 
-template <int KW, int PB, int HS>
+template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS>
 int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
     const int G = P.nsides * P.Q;
     const uint32_t bins = 1u << P.bits;
@@ -167,7 +168,7 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
     plan_units_kernel<<<1, PLAN_THREADS, 0, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
-    histogram_kernel<KW, PB, HS><<<P.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    histogram_kernel<KW, PB, HS, IN_AOS><<<P.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_HIST_END + 4 * pass, stream);
     seg_scan_kernel<<<G, PART_THREADS, 0, stream>>>(P);
@@ -177,20 +178,20 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
     unit_scan_kernel<<<bins, PLAN_THREADS, us_smem, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCAN_END + 4 * pass, stream);
-    constexpr int ITEMS = scatter_items<KW, PB, HS>();
-    const size_t sc_smem = ScatterSmem<KW, PB, HS, ITEMS>::bytes(bins);
-    VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, ITEMS>, sc_smem));
-    scatter_kernel<KW, PB, HS, ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
+    constexpr int ITEMS = scatter_items<KW, PB, HS, IN_AOS>();
+    const size_t sc_smem = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS>::bytes(bins);
+    VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS>, sc_smem));
+    scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCATTER_END + 4 * pass, stream);
     if (ctx) ctx->launches += 5;
     return VJ_OK;
 }
 
-template <int KW, int PB, int HS>
+template <int KW, int PB, int HS, bool AOS>
 int probe_grid(const DeviceInfo &info, size_t smem, int *grid) {
     int per_sm = 0;
-    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS>, PROBE_THREADS, smem));
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS>, PROBE_THREADS, smem));
     if (per_sm < 1) per_sm = 1;
     *grid = info.sms * per_sm;
     return VJ_OK;
@@ -208,26 +209,37 @@ struct JoinRun {
     uint32_t *d_error;
     // probe inputs prepared by the partition passes
     ProbeParams probe;
+    bool aos;          // probe reads row-contiguous partition buffers
     size_t probe_smem;
     int probe_grid;
 };
+
+template <int KW, int PB, int HS, bool AOS>
+int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
+    run->aos = AOS;
+    run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
+    VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS>, run->probe_smem));
+    return probe_grid<KW, PB, HS, AOS>(ctx->info, run->probe_smem, &run->probe_grid);
+}
 
 // Everything up to (not including) the probe launch. Returns probe parameters whose
 // output fields the caller fills in.
 template <int KW, int PB, int HS>
 int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, cudaStream_t stream, JoinRun *run) {
-    const size_t row_bytes = (size_t)KW * 4 + PB + (HS ? HS : 0);
+    using L = Layout<KW, PB, HS>;
     const int bins0 = 1 << pl.bits[0];
     const int bins1 = 1 << pl.bits[1];
     const int G0 = 2, G1 = 2 * bins0;
     const int np = pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1);
 
-    // ---- workspace layout (dry run, then carve)
+    // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
     const uint64_t item_cap = (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
-    auto layout = [&](Carver &c, void **bufA, void **bufB, PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **item_part, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
-        const size_t table_bytes = ((size_t)in.rows[0] + in.rows[1]) * row_bytes + 4 * 256;
-        *bufA = pl.passes >= 1 ? c.take<char>(table_bytes) : nullptr;
-        *bufB = pl.passes >= 2 ? c.take<char>(table_bytes) : nullptr;
+    auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **item_part, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
+        for (int pass = 0; pass < 2; pass++) {
+            for (int sd = 0; sd < 2; sd++) {
+                bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
+            }
+        }
         if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, pl.max_units[0]);
         if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, pl.max_units[1]);
         *item_begin = c.take<uint32_t>((size_t)np + 2);
@@ -236,50 +248,32 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         *out_count = c.take<unsigned long long>(1);
         *error = c.take<uint32_t>(1);
     };
-    void *bufA, *bufB;
+    void *bufs[2][2];
     PassBufs pb0{}, pb1{};
     uint32_t *item_begin, *item_part, *ticket, *error;
     unsigned long long *out_count;
     Carver dry;
-    layout(dry, &bufA, &bufB, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
+    layout(dry, bufs, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
     void *ws = nullptr;
     VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
     Carver c;
     c.base = (char *)ws;
-    layout(c, &bufA, &bufB, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
+    layout(c, bufs, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
     VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
     ctx->launches = 0;
 
-    // Column arrays of a partitioned copy: [R keys | S keys | R pay | S pay | R hash | S hash]
-    auto columns = [&](char *buf, void *keys[2], void *pay[2], void *hash[2]) {
-        Carver cc;
-        cc.base = buf;
-        keys[0] = cc.take<char>((size_t)in.rows[0] * KW * 4, 16);
-        keys[1] = cc.take<char>((size_t)in.rows[1] * KW * 4, 16);
-        pay[0] = cc.take<char>((size_t)in.rows[0] * PB, 16);
-        pay[1] = cc.take<char>((size_t)in.rows[1] * PB, 16);
-        hash[0] = HS ? cc.take<char>((size_t)in.rows[0] * HS, 16) : nullptr;
-        hash[1] = HS ? cc.take<char>((size_t)in.rows[1] * HS, 16) : nullptr;
-    };
-
-    const void *cur_keys[2] = {in.keys[0], in.keys[1]};
-    const void *cur_pay[2] = {in.pay[0], in.pay[1]};
-    const void *cur_hash[2] = {in.hash[0], in.hash[1]};
     const uint32_t *seg_begin = nullptr, *seg_end = nullptr;
     int Q = 1;
     int consumed_bits = 0;
     for (int pass = 0; pass < pl.passes; pass++) {
-        void *ok[2], *op[2], *oh[2];
-        columns((char *)(pass == 0 ? bufA : bufB), ok, op, oh);
         PassParams P{};
-        for (int s = 0; s < 2; s++) {
-            P.side[s].keys_in = cur_keys[s];
-            P.side[s].pay_in = cur_pay[s];
-            P.side[s].hash_in = cur_hash[s];
-            P.side[s].keys_out = ok[s];
-            P.side[s].pay_out = op[s];
-            P.side[s].hash_out = oh[s];
-            P.side[s].rows = in.rows[s];
+        for (int sd = 0; sd < 2; sd++) {
+            P.side[sd].keys_in = in.keys[sd];
+            P.side[sd].pay_in = in.pay[sd];
+            P.side[sd].hash_in = in.hash[sd];
+            P.side[sd].rows_in = pass > 0 ? bufs[pass - 1][sd] : nullptr;
+            P.side[sd].rows_out = bufs[pass][sd];
+            P.side[sd].rows = in.rows[sd];
         }
         P.nsides = 2;
         P.Q = Q;
@@ -293,11 +287,10 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         P.min_unit_rows = 4096;
         P.error = error;
         const PassBufs &pb = pass == 0 ? pb0 : pb1;
-        VJ_TRY((run_pass<KW, PB, HS>(ctx, pass, P, pb, stream)));
-        for (int s = 0; s < 2; s++) {
-            cur_keys[s] = ok[s];
-            cur_pay[s] = op[s];
-            cur_hash[s] = oh[s];
+        if (pass == 0) {
+            VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, pass, P, pb, stream)));
+        } else {
+            VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, pass, P, pb, stream)));
         }
         seg_begin = pb.part_begin;
         seg_end = pb.part_end;
@@ -305,15 +298,18 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     }
 
     ProbeParams Pq{};
-    Pq.r_keys = cur_keys[0];
-    Pq.r_pay = cur_pay[0];
-    Pq.r_hash = cur_hash[0];
-    Pq.s_keys = cur_keys[1];
-    Pq.s_pay = cur_pay[1];
-    Pq.s_hash = cur_hash[1];
+    Pq.r_keys = in.keys[0];
+    Pq.r_pay = in.pay[0];
+    Pq.r_hash = in.hash[0];
+    Pq.s_keys = in.keys[1];
+    Pq.s_pay = in.pay[1];
+    Pq.s_hash = in.hash[1];
     if (pl.passes == 0) {
+        Pq.r_rows_in = Pq.s_rows_in = nullptr;
         Pq.r_begin = Pq.r_end = Pq.s_begin = Pq.s_end = nullptr;
     } else {
+        Pq.r_rows_in = bufs[pl.passes - 1][0];
+        Pq.s_rows_in = bufs[pl.passes - 1][1];
         Pq.r_begin = seg_begin;
         Pq.r_end = seg_end;
         Pq.s_begin = seg_begin + np;
@@ -326,6 +322,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.schunk = pl.schunk;
     Pq.outcap = pl.outcap;
     Pq.sub_rows = pl.sub;
+    // slot bits: the 14 bits right below the partition bits (tables hold at most 2^14 slots)
+    Pq.slot_shift = 64 - (pl.bits[0] + pl.bits[1]) - 14;
     Pq.item_begin = item_begin;
     Pq.item_part = item_part;
     Pq.item_cap = (uint32_t)(item_cap < 0xffffffffull ? item_cap : 0xffffffffull);
@@ -336,10 +334,10 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     run->probe = Pq;
     run->d_out_count = out_count;
     run->d_error = error;
-    run->probe_smem = ProbeSmem<KW, PB, HS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
-    VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS>, run->probe_smem));
-    VJ_TRY((probe_grid<KW, PB, HS>(ctx->info, run->probe_smem, &run->probe_grid)));
-    return VJ_OK;
+    if (pl.passes == 0) {
+        return probe_setup<KW, PB, HS, false>(ctx, pl, run);
+    }
+    return probe_setup<KW, PB, HS, true>(ctx, pl, run);
 }
 
 template <int KW, int PB, int HS>
@@ -347,7 +345,11 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
     profile_mark(ctx, PM_PROBE_BEGIN, stream);
     plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
     VJ_CUDA(cudaGetLastError());
-    probe_kernel<KW, PB, HS><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+    if (run.aos) {
+        probe_kernel<KW, PB, HS, true><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+    } else {
+        probe_kernel<KW, PB, HS, false><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+    }
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_PROBE_END, stream);
     ctx->launches += 2;
@@ -491,6 +493,8 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     P.side[0].keys_in = in->keys;
     P.side[0].pay_in = in->payloads;
     P.side[0].hash_in = hashes_in;
+    P.side[0].rows_in = nullptr;
+    P.side[0].rows_out = nullptr;
     P.side[0].keys_out = keys_out;
     P.side[0].pay_out = pay_out;
     P.side[0].hash_out = hash_out;
@@ -505,7 +509,7 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     P.min_unit_rows = 4096;
     P.error = derr;
     if (in->rows > 0) {
-        VJ_TRY((run_pass<KW, PB, HS>(ctx, 0, P, pb, stream)));
+        VJ_TRY((run_pass<KW, PB, HS, false, false>(ctx, 0, P, pb, stream)));
     } else {
         VJ_CUDA(cudaMemsetAsync(pb.part_begin, 0, bins * sizeof(uint32_t), stream));
         VJ_CUDA(cudaMemsetAsync(pb.part_end, 0, bins * sizeof(uint32_t), stream));

@@ -1,10 +1,12 @@
 // vj_join_kernels.cuh -- radix partition and build/probe kernels of the join path.
 //
-// Data layout (HBM): every table is columnar -- a key array of rows of KW 32-bit words and
-// a payload array of PB-byte values (plus, for the reference-compatible entry points, a
-// hash array). Partition passes write the same layout into workspace buffers, grouped by
-// bucket. Nothing is materialised per row besides the tuple itself: the partitioning hash
-// is recomputed from the key in every kernel (a few integer ops per row).
+// Data layout (HBM). Caller tables are columnar: a key array of rows of KW 32-bit words, a
+// payload array of PB-byte values and, for the reference-compatible entry points, a hash
+// array. The partition passes of a join write row-contiguous buffers (one "row" = key,
+// payload[, hash], Layout::STRIDE bytes), so that each bucket run of a tile is one
+// contiguous burst and one bulk copy fetches a chunk of rows. Nothing else is
+// materialised per row: the partitioning hash is recomputed from the key in every kernel
+// (a few integer ops per row).
 //
 // A pass over a set of "segments" (contiguous row ranges, e.g. the partitions of the
 // previous pass) runs five kernels, none of which waits on another block:
@@ -12,12 +14,14 @@
 //   histogram    per-unit bucket counts in shared memory
 //   seg_scan     per-segment exclusive prefix over buckets -> partition boundaries
 //   unit_scan    per-bucket prefix over units -> each unit's write cursor per bucket
-//   scatter      each unit stages a tile of rows in shared memory sorted by bucket and
-//                writes every bucket's run as one contiguous burst
+//   scatter      bulk copies stream tiles of a unit into shared memory (double
+//                buffered); each tile is ranked by bucket, sorted in shared memory and
+//                written out as one contiguous run per bucket
 // The probe stage plans (partition, build chunk, probe chunk) work items and runs a
-// persistent kernel that takes items from an atomic ticket, builds an open-addressing
-// table of the build chunk in shared memory and streams the probe chunk through it,
-// staging output pairs in shared memory and writing them out in contiguous blocks.
+// persistent kernel that takes items from an atomic ticket, bulk-copies the build chunk
+// and builds an open-addressing table of its row indices in shared memory, then streams
+// the probe chunk through it in bulk-copied sub-chunks (double buffered), staging output
+// pairs in shared memory and writing them out in contiguous blocks.
 #pragma once
 
 #include "vj_internal.cuh"
@@ -25,24 +29,40 @@
 namespace vj {
 
 constexpr int MAX_RADIX_BITS = 12;
-constexpr int PART_THREADS = 256;
-constexpr int PROBE_THREADS = 256;
-constexpr int PROBE_ITEMS = 4;
+constexpr int PART_THREADS = 512;
+constexpr int PROBE_THREADS = 512;
 constexpr int PLAN_THREADS = 1024;
 
 struct HashSpec {
     int algo;       // VJ_HASH_* when the hash is recomputed from the key
     int hash_bits;  // 32 or 64
-    int mix;        // 1: extract bits from fmix64(hash), 0: from the raw hash
+    int mix;        // 1: extract bits from mix_hash(hash), 0: from the raw hash
+};
+
+constexpr int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
+// Row-contiguous layout of a partition buffer row.
+template <int KW, int PB, int HS>
+struct Layout {
+    static constexpr int KB = KW * 4;
+    static constexpr int PAY_OFF = round_up(KB, PB);
+    static constexpr int HASH_OFF = HS ? round_up(PAY_OFF + PB, HS) : PAY_OFF + PB;
+    static constexpr int STRIDE = round_up(HASH_OFF + HS, 8);
 };
 
 struct Side {
+    // columnar input (a caller's table)
     const void *keys_in;
     const void *pay_in;
-    const void *hash_in;  // HS != 0 only
+    const void *hash_in;   // HS != 0 only
+    // row-contiguous input (the previous pass's output)
+    const void *rows_in;
+    // row-contiguous output (a join's partition buffer) ...
+    void *rows_out;
+    // ... or columnar output (vj_partition writes the caller's swap columns)
     void *keys_out;
     void *pay_out;
-    void *hash_out;       // HS != 0 only (may be null: hashes not moved)
+    void *hash_out;        // HS != 0 only (may be null: hashes not moved)
     uint32_t rows;
 };
 
@@ -69,19 +89,21 @@ struct PassParams {
 };
 
 struct ProbeParams {
-    const void *r_keys, *r_pay, *r_hash;
-    const void *s_keys, *s_pay, *s_hash;
+    // columnar (unpartitioned) or row-contiguous (partitioned) sources of both tables
+    const void *r_keys, *r_pay, *r_hash, *r_rows_in;
+    const void *s_keys, *s_pay, *s_hash, *s_rows_in;
     const uint32_t *r_begin, *r_end;  // [np]; null: one partition = whole table
     const uint32_t *s_begin, *s_end;
     uint32_t r_rows, s_rows;
     int np;
-    uint32_t rcap;     // build rows per item (table capacity = 2*rcap rounded up to pow2)
-    uint32_t schunk;   // probe rows per item
-    uint32_t outcap;   // staged output pairs per block
+    uint32_t rcap;         // build rows per item (a power of two; table capacity <= 2*rcap)
+    uint32_t schunk;       // probe rows per item
+    uint32_t outcap;       // staged output pairs per block
     uint32_t *item_begin;  // [np+2]: prefix, total, and whether item_part is filled
     uint32_t *item_part;   // [item_cap]: partition of each item
     uint32_t item_cap;
     uint32_t sub_rows;     // probe rows per bulk copy
+    int slot_shift;        // table slot = (mix_hash(hash) >> slot_shift) & (capacity - 1)
     uint32_t *ticket;
     unsigned long long *out_count;
     void *out;
@@ -128,6 +150,15 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T *total) {
     if (total) *total = warp_sums[nwarps - 1];
     __syncthreads();
     return result;
+}
+
+// One thread polls the mbarrier, the block waits on a barrier behind it (the barrier
+// orders the other threads' reads after the poller's acquire). Returns false for every
+// thread if the bounded poll ran out.
+__device__ __forceinline__ bool block_wait(uint64_t *bar, uint32_t parity) {
+    int fail = 0;
+    if (threadIdx.x == 0) fail = !mbar_wait(bar, parity);
+    return __syncthreads_or(fail) == 0;
 }
 
 // Generic (non-FNV) row hash, out of line.
@@ -183,37 +214,103 @@ __device__ __forceinline__ uint64_t row_hash(const Key<KW> &k, const HashSpec &h
     return row_hash_generic(w, KW, hs.algo, hs.hash_bits);
 }
 
-// A row while it moves through a kernel. HS: 0 = hash recomputed from the key, 4/8 = hash
-// read from (and carried with) a u32/u64 hash array.
-template <int KW, int PB, int HS>
-struct Row {
-    using P = typename PayloadType<PB>::T;
-    Key<KW> k;
-    P p;
-    uint64_t h;   // hash as given or recomputed (before mixing)
-};
-
-template <int HS>
-__device__ __forceinline__ uint64_t load_hash(const void *base, uint64_t row) {
-    if (HS == 8) return __ldcs((const unsigned long long *)base + row);
-    return (uint64_t)__ldcs((const uint32_t *)base + row);
-}
-
-template <int KW, int PB, int HS>
-__device__ __forceinline__ void load_row(const void *keys, const void *pay, const void *hashes, uint64_t i, const HashSpec &hs, Row<KW, PB, HS> &r) {
-    using P = typename PayloadType<PB>::T;
-    r.k = load_key_stream<KW>(keys, i);
-    r.p = __ldcs((const P *)pay + i);
-    if (HS) {
-        r.h = load_hash<HS>(hashes, i);
-    } else {
-        r.h = row_hash<KW>(r.k, hs);
-    }
+// Multiplicative (Fibonacci) mix: its top bits depend on every bit of the hash. The join
+// cuts its partitions from the top bits, most significant first, and takes the table slot
+// from the bits right below them, so rows of one partition still spread over the table.
+__device__ __forceinline__ uint64_t mix_hash(uint64_t h) {
+    return h * 0x9e3779b97f4a7c15ull;
 }
 
 __device__ __forceinline__ uint64_t bucket_hash(uint64_t h, const HashSpec &hs) {
-    return hs.mix ? fmix64(h) : h;
+    return hs.mix ? mix_hash(h) : h;
 }
+
+template <int HS>
+__device__ __forceinline__ uint64_t read_hash(const unsigned char *p) {
+    if (HS == 8) return *(const unsigned long long *)p;
+    return *(const uint32_t *)p;
+}
+
+// ------------------------------------------------------------------ rows in shared memory
+//
+// A chunk of rows [a, b) of a table is copied into shared memory by bulk copies of the
+// 16-byte aligned windows that cover it: one window for a row-contiguous source, one per
+// column for a columnar source. The view gives key / payload / hash of row a + i.
+
+template <int KW, int PB, int HS, bool AOS>
+struct Chunk {
+    using L = Layout<KW, PB, HS>;
+    using P = typename PayloadType<PB>::T;
+    __host__ __device__ static constexpr size_t col(size_t bytes) { return (bytes + 32 + 15) / 16 * 16; }
+    __host__ __device__ static constexpr size_t bytes(uint32_t rows) {
+        return AOS ? col((size_t)rows * L::STRIDE) : col((size_t)rows * L::KB) + col((size_t)rows * PB) + (HS ? col((size_t)rows * HS) : 0);
+    }
+    // shared-memory views
+    const unsigned char *k;
+    const unsigned char *p;
+    const unsigned char *h;
+    __device__ __forceinline__ Key<KW> key(uint32_t i) const { return key_from_smem<KW>(k + (size_t)i * (AOS ? L::STRIDE : L::KB)); }
+    __device__ __forceinline__ P pay(uint32_t i) const { return *(const P *)(p + (size_t)i * (AOS ? L::STRIDE : PB)); }
+    __device__ __forceinline__ uint64_t hash(uint32_t i) const { return read_hash<HS>(h + (size_t)i * (AOS ? L::STRIDE : HS)); }
+    __device__ __forceinline__ uint64_t h_of(uint32_t i, const HashSpec &hs) const { return HS ? hash(i) : row_hash<KW>(key(i), hs); }
+    // copy of row i as raw bytes into `dst` (row-contiguous layout)
+    __device__ __forceinline__ void copy_row(uint32_t i, unsigned char *dst) const {
+        if (AOS) {
+            const unsigned char *src = k + (size_t)i * L::STRIDE;
+#pragma unroll
+            for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(dst + o) = *(const uint2 *)(src + o);
+        } else {
+            key_to_smem<KW>(dst, key(i));
+            *(P *)(dst + L::PAY_OFF) = pay(i);
+            if (HS == 8) *(unsigned long long *)(dst + L::HASH_OFF) = hash(i);
+            if (HS == 4) *(uint32_t *)(dst + L::HASH_OFF) = (uint32_t)hash(i);
+        }
+    }
+
+    // Issue the copies of rows [a, b) into `buf` (capacity `cap` rows); deltas[0..2] receive
+    // the offsets of row a inside the windows. Called by one thread.
+    __device__ __forceinline__ static void issue(const void *keys, const void *pay, const void *hash, const void *rows, uint32_t a, uint32_t b, uint32_t cap, unsigned char *buf, uint64_t *bar,
+                                                 uint32_t *deltas) {
+        if (AOS) {
+            const ColWindow w = col_window(rows, L::STRIDE, a, b);
+            deltas[0] = w.delta;
+            mbar_arrive_expect_tx(bar, w.bytes);
+            bulk_g2s(buf, w.src, w.bytes, bar);
+        } else {
+            const ColWindow wk = col_window(keys, L::KB, a, b);
+            const ColWindow wp = col_window(pay, PB, a, b);
+            uint32_t total = wk.bytes + wp.bytes;
+            ColWindow wh{nullptr, 0, 0};
+            if (HS) {
+                wh = col_window(hash, HS, a, b);
+                total += wh.bytes;
+            }
+            deltas[0] = wk.delta;
+            deltas[1] = wp.delta;
+            deltas[2] = wh.delta;
+            const size_t kcol = col((size_t)cap * L::KB), pcol = col((size_t)cap * PB);
+            mbar_arrive_expect_tx(bar, total);
+            bulk_g2s(buf, wk.src, wk.bytes, bar);
+            bulk_g2s(buf + kcol, wp.src, wp.bytes, bar);
+            if (HS) bulk_g2s(buf + kcol + pcol, wh.src, wh.bytes, bar);
+        }
+    }
+
+    __device__ __forceinline__ static Chunk view(const unsigned char *buf, uint32_t cap, const uint32_t *deltas) {
+        Chunk c;
+        if (AOS) {
+            c.k = buf + deltas[0];
+            c.p = c.k + L::PAY_OFF;
+            c.h = c.k + L::HASH_OFF;
+        } else {
+            const size_t kcol = col((size_t)cap * L::KB), pcol = col((size_t)cap * PB);
+            c.k = buf + deltas[0];
+            c.p = buf + kcol + deltas[1];
+            c.h = buf + kcol + pcol + deltas[2];
+        }
+        return c;
+    }
+};
 
 // ------------------------------------------------------------------ partition kernels
 
@@ -261,7 +358,33 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_units_kernel(PassParams P) 
     }
 }
 
-template <int KW, int PB, int HS>
+// Hash of row i read straight from global memory (histogram pass).
+template <int KW, int PB, int HS, bool AOS>
+__device__ __forceinline__ uint64_t global_row_hash(const Side &S, uint32_t i, const HashSpec &hs) {
+    using L = Layout<KW, PB, HS>;
+    if (AOS) {
+        const unsigned char *row = (const unsigned char *)S.rows_in + (size_t)i * L::STRIDE;
+        if (HS == 8) return __ldcs((const unsigned long long *)(row + L::HASH_OFF));
+        if (HS == 4) return __ldcs((const uint32_t *)(row + L::HASH_OFF));
+        Key<KW> k;
+        if (KW == 1) {
+            k.w[0] = __ldcs((const uint32_t *)row);
+        } else {
+#pragma unroll
+            for (int j = 0; j < KW / 2; j++) {
+                uint2 v = __ldcs((const uint2 *)row + j);
+                k.w[2 * j] = v.x;
+                k.w[2 * j + 1] = v.y;
+            }
+        }
+        return row_hash<KW>(k, hs);
+    }
+    if (HS == 8) return __ldcs((const unsigned long long *)S.hash_in + i);
+    if (HS == 4) return __ldcs((const uint32_t *)S.hash_in + i);
+    return row_hash<KW>(load_key_stream<KW>(S.keys_in, i), hs);
+}
+
+template <int KW, int PB, int HS, bool AOS>
 __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
     extern __shared__ uint32_t s_hist[];
     const uint32_t u = blockIdx.x;
@@ -276,22 +399,13 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
     uint32_t i = U.y + threadIdx.x;
     for (; i + (UNROLL - 1) * PART_THREADS < U.z; i += UNROLL * PART_THREADS) {
         uint64_t h[UNROLL];
-        if (HS) {
 #pragma unroll
-            for (int k = 0; k < UNROLL; k++) h[k] = load_hash<HS>(S.hash_in, i + k * PART_THREADS);
-        } else {
-            Key<KW> key[UNROLL];
-#pragma unroll
-            for (int k = 0; k < UNROLL; k++) key[k] = load_key_stream<KW>(S.keys_in, i + k * PART_THREADS);
-#pragma unroll
-            for (int k = 0; k < UNROLL; k++) h[k] = row_hash<KW>(key[k], P.hs);
-        }
+        for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * PART_THREADS, P.hs);
 #pragma unroll
         for (int k = 0; k < UNROLL; k++) atomicAdd(&s_hist[(bucket_hash(h[k], P.hs) >> P.shift) & mask], 1u);
     }
     for (; i < U.z; i += PART_THREADS) {
-        uint64_t h = HS ? load_hash<HS>(S.hash_in, i) : row_hash<KW>(load_key_stream<KW>(S.keys_in, i), P.hs);
-        atomicAdd(&s_hist[(bucket_hash(h, P.hs) >> P.shift) & mask], 1u);
+        atomicAdd(&s_hist[(bucket_hash(global_row_hash<KW, PB, HS, AOS>(S, i, P.hs), P.hs) >> P.shift) & mask], 1u);
     }
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
@@ -305,7 +419,6 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
 __global__ void __launch_bounds__(PART_THREADS) seg_scan_kernel(PassParams P) {
     __shared__ uint32_t s_warp[32];
     const int g = blockIdx.x;
-    const int side = g / P.Q;
     const uint32_t bins = 1u << P.bits;
     const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
     const uint32_t b0 = threadIdx.x * per;
@@ -314,7 +427,6 @@ __global__ void __launch_bounds__(PART_THREADS) seg_scan_kernel(PassParams P) {
     for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += tot[b];
     uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
     run += P.seg_begin ? P.seg_begin[g] : 0;
-    (void)side;
     for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
         P.part_begin[(size_t)g * bins + b] = run;
         run += tot[b];
@@ -345,64 +457,39 @@ __global__ void __launch_bounds__(PLAN_THREADS) unit_scan_kernel(PassParams P) {
     }
 }
 
-// Shared memory of the scatter kernel: two input tiles filled by bulk copies (each column
-// as its 16-byte aligned window), the bucket-sorted output tile, bucket ids and counters.
-template <int KW, int PB, int HS, int ITEMS>
+// Shared memory of the scatter kernel: two input tiles filled by bulk copies, the
+// bucket-sorted output tile (row-contiguous), bucket ids and counters.
+template <int KW, int PB, int HS, bool IN_AOS, int ITEMS>
 struct ScatterSmem {
+    using L = Layout<KW, PB, HS>;
     static constexpr int T = PART_THREADS * ITEMS;
-    static constexpr size_t col(size_t bytes) { return (bytes + 32 + 15) / 16 * 16; }
-    static constexpr size_t KEYS = col((size_t)T * KW * 4);
-    static constexpr size_t PAY = col((size_t)T * PB);
-    static constexpr size_t HASH = HS ? col((size_t)T * HS) : 0;
-    static constexpr size_t IN_BUF = KEYS + PAY + HASH;
-    static constexpr size_t OUT = (size_t)T * (KW * 4 + PB + (HS ? 8 : 0) + 2);
+    static constexpr size_t IN_BUF = Chunk<KW, PB, HS, IN_AOS>::bytes(T);
+    static constexpr size_t OUT = (size_t)T * (L::STRIDE + 2);
     static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 3 * 4; }
 };
 
-// Rows per thread of a scatter tile: the largest of 8, 4, 2 whose block (with 2^10 bins)
+// Rows per thread of a scatter tile: the largest of 4, 2, 1 whose block (with 2^10 bins)
 // stays within about half of an SM's shared memory, so two blocks fit per SM (wider
 // passes, up to 2^12 bins, stay below the 227 KB block limit with one block per SM).
-template <int KW, int PB, int HS>
+template <int KW, int PB, int HS, bool IN_AOS>
 constexpr int scatter_items() {
-    return ScatterSmem<KW, PB, HS, 8>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, 8>::OUT + 16 + 1024 * 12 <= 113 * 1024   ? 8
-           : ScatterSmem<KW, PB, HS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, 4>::OUT + 16 + 1024 * 12 <= 113 * 1024 ? 4
-                                                                                                                     : 2;
+    return ScatterSmem<KW, PB, HS, IN_AOS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 4>::OUT + 16 + 1024 * 12 <= 113 * 1024   ? 4
+           : ScatterSmem<KW, PB, HS, IN_AOS, 2>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 2>::OUT + 16 + 1024 * 12 <= 113 * 1024 ? 2
+                                                                                                                                     : 1;
 }
 
-// One tile of a unit: rows [a, b) of one side, copied column by column into input buffer
-// `buf` (issued by one thread).
-template <int KW, int PB, int HS, int ITEMS>
-__device__ __forceinline__ void scatter_issue(const Side &S, uint32_t a, uint32_t b, unsigned char *inb, uint64_t *bar, uint32_t *delta) {
-    using SM = ScatterSmem<KW, PB, HS, ITEMS>;
-    const ColWindow wk = col_window(S.keys_in, KW * 4, a, b);
-    const ColWindow wp = col_window(S.pay_in, PB, a, b);
-    uint32_t total = wk.bytes + wp.bytes;
-    ColWindow wh{nullptr, 0, 0};
-    if (HS) {
-        wh = col_window(S.hash_in, HS, a, b);
-        total += wh.bytes;
-    }
-    delta[0] = wk.delta;
-    delta[1] = wp.delta;
-    delta[2] = wh.delta;
-    mbar_arrive_expect_tx(bar, total);
-    bulk_g2s(inb, wk.src, wk.bytes, bar);
-    bulk_g2s(inb + SM::KEYS, wp.src, wp.bytes, bar);
-    if (HS) bulk_g2s(inb + SM::KEYS + SM::PAY, wh.src, wh.bytes, bar);
-}
-
-template <int KW, int PB, int HS, int ITEMS>
+template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS>
 __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
+    using L = Layout<KW, PB, HS>;
+    using C = Chunk<KW, PB, HS, IN_AOS>;
     using Pt = typename PayloadType<PB>::T;
-    using SM = ScatterSmem<KW, PB, HS, ITEMS>;
+    using SM = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS>;
     constexpr int T = SM::T;
     extern __shared__ __align__(16) unsigned char s_raw[];
     uint64_t *bar = (uint64_t *)s_raw;
     unsigned char *inb0 = s_raw + 16;
-    unsigned char *out_keys = inb0 + 2 * SM::IN_BUF;
-    Pt *out_pay = (Pt *)(out_keys + (size_t)T * KW * 4);
-    unsigned long long *out_hash = (unsigned long long *)((unsigned char *)out_pay + (size_t)T * PB);
-    uint16_t *st_b = (uint16_t *)((unsigned char *)out_hash + (HS ? (size_t)T * 8 : 0));
+    unsigned char *out_rows = inb0 + 2 * SM::IN_BUF;
+    uint16_t *st_b = (uint16_t *)(out_rows + (size_t)T * L::STRIDE);
     const uint32_t bins = 1u << P.bits;
     uint32_t *s_run = (uint32_t *)(st_b + T);
     uint32_t *s_cnt = s_run + bins;
@@ -428,7 +515,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     if (threadIdx.x == 0) {
         for (uint32_t k = 0; k < 2 && k < ntiles; k++) {
             const uint32_t a = U.y + k * T;
-            scatter_issue<KW, PB, HS, ITEMS>(S, a, min(U.z, a + T), inb0 + k * SM::IN_BUF, &bar[k], s_delta[k]);
+            C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T), T, inb0 + k * SM::IN_BUF, &bar[k], s_delta[k]);
         }
     }
 
@@ -437,27 +524,22 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         const uint32_t tile = U.y + k * T;
         const uint32_t nt = min(U.z - tile, (uint32_t)T);
         for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_cnt[b] = 0;
-        const bool ok = mbar_wait(&bar[buf], (k >> 1) & 1);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicOr(P.error, 4u);
-            // let any other copy of this block land before leaving
-            if (k + 1 < ntiles) mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
+        if (!block_wait(&bar[buf], (k >> 1) & 1)) {
+            if (threadIdx.x == 0) {
+                atomicOr(P.error, 4u);
+                // let the other copy of this block land before leaving
+                if (k + 1 < ntiles) mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
+            }
             return;
         }
-        const unsigned char *kc = inb0 + buf * SM::IN_BUF + s_delta[buf][0];
-        const Pt *pc = (const Pt *)(inb0 + buf * SM::IN_BUF + SM::KEYS + s_delta[buf][1]);
-        const unsigned char *hc = inb0 + buf * SM::IN_BUF + SM::KEYS + SM::PAY + s_delta[buf][2];
+        const C in = C::view(inb0 + buf * SM::IN_BUF, T, s_delta[buf]);
         uint32_t bk[ITEMS];
         uint32_t rk[ITEMS];
 #pragma unroll
         for (int j = 0; j < ITEMS; j++) {
             const uint32_t i = j * PART_THREADS + threadIdx.x;
             if (i < nt) {
-                uint64_t h;
-                if (HS == 8) h = ((const unsigned long long *)hc)[i];
-                else if (HS == 4) h = ((const uint32_t *)hc)[i];
-                else h = row_hash<KW>(key_from_smem<KW>(kc + (size_t)i * KW * 4), P.hs);
-                bk[j] = (uint32_t)((bucket_hash(h, P.hs) >> P.shift) & mask);
+                bk[j] = (uint32_t)((bucket_hash(in.h_of(i, P.hs), P.hs) >> P.shift) & mask);
                 rk[j] = atomicAdd(&s_cnt[bk[j]], 1u);
             }
         }
@@ -477,10 +559,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
             const uint32_t i = j * PART_THREADS + threadIdx.x;
             if (i < nt) {
                 const uint32_t pos = s_start[bk[j]] + rk[j];
-                key_to_smem<KW>(out_keys + (size_t)pos * KW * 4, key_from_smem<KW>(kc + (size_t)i * KW * 4));
-                out_pay[pos] = pc[i];
-                if (HS == 8) out_hash[pos] = ((const unsigned long long *)hc)[i];
-                else if (HS == 4) out_hash[pos] = ((const uint32_t *)hc)[i];
+                in.copy_row(i, out_rows + (size_t)pos * L::STRIDE);
                 st_b[pos] = (uint16_t)bk[j];
             }
         }
@@ -488,16 +567,28 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         if (threadIdx.x == 0 && k + 2 < ntiles) {
             fence_proxy_async();
             const uint32_t a = U.y + (k + 2) * T;
-            scatter_issue<KW, PB, HS, ITEMS>(S, a, min(U.z, a + T), inb0 + buf * SM::IN_BUF, &bar[buf], s_delta[buf]);
+            C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T), T, inb0 + buf * SM::IN_BUF, &bar[buf], s_delta[buf]);
         }
         for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
             const uint32_t b = st_b[i];
             const uint32_t dst = s_run[b] + i - s_start[b];
-            store_key<KW>(S.keys_out, dst, key_from_smem<KW>(out_keys + (size_t)i * KW * 4));
-            ((Pt *)S.pay_out)[dst] = out_pay[i];
-            if (HS && S.hash_out) {
-                if (HS == 8) ((unsigned long long *)S.hash_out)[dst] = out_hash[i];
-                else ((uint32_t *)S.hash_out)[dst] = (uint32_t)out_hash[i];
+            const unsigned char *row = out_rows + (size_t)i * L::STRIDE;
+            if (OUT_AOS) {
+                unsigned char *g = (unsigned char *)S.rows_out + (size_t)dst * L::STRIDE;
+                if (L::STRIDE % 16 == 0) {
+#pragma unroll
+                    for (int o = 0; o < L::STRIDE; o += 16) *(uint4 *)(g + o) = *(const uint4 *)(row + o);
+                } else {
+#pragma unroll
+                    for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(g + o) = *(const uint2 *)(row + o);
+                }
+            } else {
+                store_key<KW>(S.keys_out, dst, key_from_smem<KW>(row));
+                ((Pt *)S.pay_out)[dst] = *(const Pt *)(row + L::PAY_OFF);
+                if (HS && S.hash_out) {
+                    if (HS == 8) ((unsigned long long *)S.hash_out)[dst] = *(const unsigned long long *)(row + L::HASH_OFF);
+                    else ((uint32_t *)S.hash_out)[dst] = *(const uint32_t *)(row + L::HASH_OFF);
+                }
             }
         }
         __syncthreads();
@@ -559,65 +650,15 @@ struct Pair<8> {
     static __device__ __forceinline__ T make(unsigned long long a, unsigned long long b) { return make_ulonglong2(a, b); }
 };
 
-// Shared memory of the probe kernel: the build chunk as copied (each column as its
-// 16-byte aligned window), the open-addressing table of build-row indices, two probe
-// sub-chunks filled by bulk copies, and the output staging area.
-template <int KW, int PB, int HS>
+// Shared memory of the probe kernel: barriers, the build chunk as copied, the table of
+// build-row indices, two probe sub-chunks and the output staging area.
+template <int KW, int PB, int HS, bool AOS>
 struct ProbeSmem {
-    __host__ __device__ static size_t col(size_t bytes) { return (bytes + 32 + 15) / 16 * 16; }
-    __host__ __device__ static size_t rows_bytes(uint32_t rows) { return col((size_t)rows * KW * 4) + col((size_t)rows * PB) + (HS ? col((size_t)rows * HS) : 0); }
+    using C = Chunk<KW, PB, HS, AOS>;
     __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t sub, uint32_t outcap) {
-        return 32 + rows_bytes(rcap) + (size_t)tcap * 4 + 2 * rows_bytes(sub) + (size_t)outcap * 2 * PB;
+        return 32 + C::bytes(rcap) + (size_t)tcap * 4 + 2 * C::bytes(sub) + (size_t)outcap * 2 * PB;
     }
 };
-
-// Column views of a chunk copied into shared memory.
-template <int KW, int PB, int HS>
-struct SmemRows {
-    const unsigned char *keys;
-    const typename PayloadType<PB>::T *pay;
-    const unsigned char *hash;
-    __device__ __forceinline__ Key<KW> key(uint32_t i) const { return key_from_smem<KW>(keys + (size_t)i * KW * 4); }
-    __device__ __forceinline__ uint64_t h(uint32_t i, const HashSpec &hs) const {
-        if (HS == 8) return ((const unsigned long long *)hash)[i];
-        if (HS == 4) return ((const uint32_t *)hash)[i];
-        return row_hash<KW>(key(i), hs);
-    }
-};
-
-// Issue the copies of rows [a, b) of one table into `dst` (sized for `cap` rows); the
-// returned views are valid once `bar` completes.
-template <int KW, int PB, int HS>
-__device__ __forceinline__ void probe_issue(const void *keys, const void *pay, const void *hash, uint32_t a, uint32_t b, uint32_t cap, unsigned char *dst, uint64_t *bar, uint32_t *delta) {
-    using SM = ProbeSmem<KW, PB, HS>;
-    const ColWindow wk = col_window(keys, KW * 4, a, b);
-    const ColWindow wp = col_window(pay, PB, a, b);
-    uint32_t total = wk.bytes + wp.bytes;
-    ColWindow wh{nullptr, 0, 0};
-    if (HS) {
-        wh = col_window(hash, HS, a, b);
-        total += wh.bytes;
-    }
-    delta[0] = wk.delta;
-    delta[1] = wp.delta;
-    delta[2] = wh.delta;
-    const size_t kcol = SM::col((size_t)cap * KW * 4), pcol = SM::col((size_t)cap * PB);
-    mbar_arrive_expect_tx(bar, total);
-    bulk_g2s(dst, wk.src, wk.bytes, bar);
-    bulk_g2s(dst + kcol, wp.src, wp.bytes, bar);
-    if (HS) bulk_g2s(dst + kcol + pcol, wh.src, wh.bytes, bar);
-}
-
-template <int KW, int PB, int HS>
-__device__ __forceinline__ SmemRows<KW, PB, HS> rows_view(const unsigned char *buf, uint32_t cap, const uint32_t *delta) {
-    using SM = ProbeSmem<KW, PB, HS>;
-    const size_t kcol = SM::col((size_t)cap * KW * 4), pcol = SM::col((size_t)cap * PB);
-    SmemRows<KW, PB, HS> v;
-    v.keys = buf + delta[0];
-    v.pay = (const typename PayloadType<PB>::T *)(buf + kcol + delta[1]);
-    v.hash = buf + kcol + pcol + delta[2];
-    return v;
-}
 
 // Write the staged pairs [0, n) to the output at a block of positions taken from the
 // global counter; positions at or past the capacity are dropped (the count still grows).
@@ -633,19 +674,19 @@ __device__ __forceinline__ void flush_pairs(const ProbeParams &Q, typename Pair<
     }
 }
 
-template <int KW, int PB, int HS>
+template <int KW, int PB, int HS, bool AOS>
 __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
+    using C = Chunk<KW, PB, HS, AOS>;
     using Pt = typename PayloadType<PB>::T;
     using PT = typename Pair<PB>::T;
-    using SM = ProbeSmem<KW, PB, HS>;
     extern __shared__ __align__(16) unsigned char s_raw[];
     const uint32_t tcap_max = 2 * Q.rcap;  // rcap is a power of two
     // layout: barriers | build chunk | table | probe sub-chunks x2 | output staging
-    uint64_t *bar = (uint64_t *)s_raw;     // [0] build chunk, [1], [2] probe sub-chunks
+    uint64_t *bar = (uint64_t *)s_raw;  // [0] build chunk, [1], [2] probe sub-chunks
     unsigned char *rbuf = s_raw + 32;
-    uint32_t *t_idx = (uint32_t *)(rbuf + SM::rows_bytes(Q.rcap));
+    uint32_t *t_idx = (uint32_t *)(rbuf + C::bytes(Q.rcap));
     unsigned char *sbuf0 = (unsigned char *)(t_idx + tcap_max);
-    const size_t sbytes = SM::rows_bytes(Q.sub_rows);
+    const size_t sbytes = C::bytes(Q.sub_rows);
     PT *stage = (PT *)(sbuf0 + 2 * sbytes);
 
     __shared__ uint32_t s_item, s_part;
@@ -653,6 +694,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
     __shared__ unsigned long long s_base;
     __shared__ uint32_t s_rdelta[3];
     __shared__ uint32_t s_sdelta[2][3];
+    __shared__ int s_dups;
     const int lane = threadIdx.x & 31;
     const uint32_t total_items = Q.item_begin[Q.np];
     const bool direct = Q.item_begin[Q.np + 1] != 0;
@@ -687,6 +729,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
             }
             s_item = it;
             s_part = p;
+            s_dups = 0;
         }
         __syncthreads();
         const uint32_t item = s_item;
@@ -707,40 +750,52 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         const uint32_t cmask = cap - 1;
 
         if (threadIdx.x == 0) {
-            probe_issue<KW, PB, HS>(Q.r_keys, Q.r_pay, Q.r_hash, r0, r1, Q.rcap, rbuf, &bar[0], s_rdelta);
+            fence_proxy_async();
+            C::issue(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, r0, r1, Q.rcap, rbuf, &bar[0], s_rdelta);
             const uint32_t sbi = s_issued & 1;
-            probe_issue<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, s0, min(s1, s0 + Q.sub_rows), Q.sub_rows, sbuf0 + sbi * sbytes, &bar[1 + sbi], s_sdelta[sbi]);
+            C::issue(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, s0, min(s1, s0 + Q.sub_rows), Q.sub_rows, sbuf0 + sbi * sbytes, &bar[1 + sbi], s_sdelta[sbi]);
         }
         s_issued++;
         for (uint32_t i = threadIdx.x; i < cap; i += PROBE_THREADS) t_idx[i] = 0;
-        bool ok = mbar_wait(&bar[0], r_loads & 1);
+        const bool ok_r = block_wait(&bar[0], r_loads & 1);
         r_loads++;
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicOr(Q.error, 4u);
-            mbar_wait(&bar[1 + ((s_issued - 1) & 1)], ((s_issued - 1) >> 1) & 1);
+        if (!ok_r) {
+            if (threadIdx.x == 0) {
+                atomicOr(Q.error, 4u);
+                mbar_wait(&bar[1 + ((s_issued - 1) & 1)], ((s_issued - 1) >> 1) & 1);
+            }
             return;
         }
-        // ---- build: table of build-row indices (+1) keyed by the mixed hash
-        const SmemRows<KW, PB, HS> R = rows_view<KW, PB, HS>(rbuf, Q.rcap, s_rdelta);
+        // ---- build: table of build-row indices (+1) keyed by the mixed hash; an equal key
+        // met on the way marks the chunk as having duplicate keys
+        const C R = C::view(rbuf, Q.rcap, s_rdelta);
         for (uint32_t i = threadIdx.x; i < nr; i += PROBE_THREADS) {
-            uint32_t slot = (uint32_t)fmix64(R.h(i, Q.hs)) & cmask;
+            const Key<KW> key = R.key(i);
+            const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
+            uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
             uint32_t tries = 0;
-            while (atomicCAS(&t_idx[slot], 0u, i + 1) != 0u) {
+            bool dup = false;
+            for (;;) {
+                const uint32_t prev = atomicCAS(&t_idx[slot], 0u, i + 1);
+                if (prev == 0u) break;
+                dup |= key_equal<KW>(R.key(prev - 1), key);
                 slot = (slot + 1) & cmask;
                 if (++tries > cap) {  // cannot happen: at most half the slots are used
                     atomicOr(Q.error, 1u);
                     break;
                 }
             }
+            if (dup) s_dups = 1;
         }
         __syncthreads();
+        const bool dups = s_dups != 0;
 
         // ---- probe the sub-chunks of this item, the next one loading meanwhile
         for (uint32_t sub = 0; sub < nsub; sub++) {
             const uint32_t sbi = s_waited & 1;
-            ok = mbar_wait(&bar[1 + sbi], (s_waited >> 1) & 1);
+            const bool ok = block_wait(&bar[1 + sbi], (s_waited >> 1) & 1);
             s_waited++;
-            if (__syncthreads_or(!ok)) {
+            if (!ok) {
                 if (threadIdx.x == 0) atomicOr(Q.error, 4u);
                 return;
             }
@@ -749,11 +804,11 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                     fence_proxy_async();
                     const uint32_t a = s0 + (sub + 1) * Q.sub_rows;
                     const uint32_t nbi = s_issued & 1;
-                    probe_issue<KW, PB, HS>(Q.s_keys, Q.s_pay, Q.s_hash, a, min(s1, a + Q.sub_rows), Q.sub_rows, sbuf0 + nbi * sbytes, &bar[1 + nbi], s_sdelta[nbi]);
+                    C::issue(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, a, min(s1, a + Q.sub_rows), Q.sub_rows, sbuf0 + nbi * sbytes, &bar[1 + nbi], s_sdelta[nbi]);
                 }
                 s_issued++;
             }
-            const SmemRows<KW, PB, HS> Sv = rows_view<KW, PB, HS>(sbuf0 + sbi * sbytes, Q.sub_rows, s_sdelta[sbi]);
+            const C Sv = C::view(sbuf0 + sbi * sbytes, Q.sub_rows, s_sdelta[sbi]);
             const uint32_t a = s0 + sub * Q.sub_rows;
             const uint32_t ns = min(s1 - a, Q.sub_rows);
             for (uint32_t base = 0; base < ns; base += PROBE_THREADS) {
@@ -764,11 +819,12 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                 uint32_t slot = 0;
                 if (active) {
                     skey = Sv.key(i);
-                    sh = Sv.h(i, Q.hs);
-                    slot = (uint32_t)fmix64(sh) & cmask;
+                    sh = HS ? Sv.hash(i) : row_hash<KW>(skey, Q.hs);
+                    slot = (uint32_t)(mix_hash(sh) >> Q.slot_shift) & cmask;
                 }
                 // Lanes walk their probe sequences in lock step; each step emits the lanes
-                // that matched with one shared-memory reservation per warp.
+                // that matched with one shared-memory reservation per warp. Without
+                // duplicate build keys a probe row stops at its first match.
                 while (__any_sync(0xffffffffu, active)) {
                     bool match = false;
                     Pt rp = 0;
@@ -777,9 +833,10 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                         if (e == 0) {
                             active = false;
                         } else {
-                            if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.h(e - 1, Q.hs) == sh)) {
+                            if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.hash(e - 1) == sh)) {
                                 match = true;
-                                rp = R.pay[e - 1];
+                                rp = R.pay(e - 1);
+                                active = dups;
                             }
                             slot = (slot + 1) & cmask;
                         }
@@ -792,7 +849,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                         pos0 = __shfl_sync(0xffffffffu, pos0, leader);
                         if (match) {
                             const uint32_t pos = pos0 + __popc(m & lanemask_lt());
-                            const Pt sp = Sv.pay[i];
+                            const Pt sp = Sv.pay(i);
                             if (pos < Q.outcap) {
                                 stage[pos] = Pair<PB>::make(rp, sp);
                             } else {
