@@ -186,7 +186,9 @@ typedef struct vj_join_options {
     int32_t build_rows;     /* build rows per shared-memory table, rounded up to a power of
                                two and capped by shared memory; 0 = largest that fits */
     int32_t probe_rows;     /* probe rows per work item; 0 = automatic */
-    int32_t reserved[6];
+    int32_t probe_threads;  /* threads per probe block (64..512, multiple of 32); 0 = automatic */
+    int32_t probe_sub_rows; /* probe rows per bulk copy (32..2048); 0 = automatic */
+    int32_t reserved[4];
 } vj_join_options;
 
 /* Join output. If pairs != NULL and capacity > 0 on entry, the caller owns the buffer (device

@@ -319,6 +319,12 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
+// Prefetch [src, src + bytes) into L2 through the bulk-copy engine (no completion to wait
+// for; src 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // The 16-byte aligned window of global memory that covers rows [a, b) of a column with
 // `cb`-byte rows starting at `base`. Bytes outside the column inside that window share a
 // 16-byte chunk with column bytes, so reading them cannot cross a page boundary.

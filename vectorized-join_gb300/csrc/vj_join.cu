@@ -39,6 +39,7 @@ struct Plan {
     uint32_t schunk = 8192;   // probe rows per work item
     uint32_t sub = 1024;      // probe rows per bulk copy
     uint32_t outcap = 1536;   // staged output pairs per block
+    int threads = PROBE_THREADS;  // probe block size
     int max_units[2] = {0, 0};
 };
 
@@ -63,7 +64,7 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     bool found = false;
     for (uint32_t sub = 1024; sub >= 256 && !found; sub >>= 1) {
         for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
-            const uint32_t outcap = sub + sub / 2;
+            const uint32_t outcap = sub;
             // sized for row-contiguous chunks, which are never smaller than columnar ones
             if (ProbeSmem<KW, PB, HS, true>::bytes(rcap, 2 * rcap, sub, outcap) <= budget && (rcap >= 1024 || sub == 256)) {
                 pl.rcap = rcap;
@@ -74,6 +75,15 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
             }
         }
     }
+    if (opt && opt->probe_threads > 0) {
+        int t = opt->probe_threads / 32 * 32;
+        pl.threads = t < 64 ? 64 : (t > PROBE_THREADS ? PROBE_THREADS : t);
+    }
+    if (opt && opt->probe_sub_rows > 0) {
+        uint32_t sub = (uint32_t)opt->probe_sub_rows;
+        pl.sub = sub < 32 ? 32 : (sub > 2048 ? 2048 : sub);
+        pl.outcap = pl.sub;
+    }
     if (opt && opt->build_rows > 0) {
         uint32_t want = 32;
         while (want < (uint32_t)opt->build_rows && want < pl.rcap) want <<= 1;
@@ -83,7 +93,7 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
         pl.schunk = (uint32_t)opt->probe_rows;
         if (pl.sub > pl.schunk) {
             pl.sub = pl.schunk < 32 ? 32 : pl.schunk;
-            pl.outcap = pl.sub + pl.sub / 2;
+            pl.outcap = pl.sub;
         }
     }
     // passes / bits: the average build partition should fill about half a table
@@ -103,7 +113,9 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
         pl.bits[0] = total_bits;
     } else {
         pl.passes = 2;
-        pl.bits[0] = (total_bits + 1) / 2;
+        // the first pass scatters over the whole table, the second within small segments:
+        // give the extra bit to the second
+        pl.bits[0] = total_bits / 2;
         pl.bits[1] = total_bits - pl.bits[0];
     }
     if (opt && (opt->flags & VJ_JOIN_FIXED_PASSES)) {
@@ -189,9 +201,9 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
 }
 
 template <int KW, int PB, int HS, bool AOS>
-int probe_grid(const DeviceInfo &info, size_t smem, int *grid) {
+int probe_grid(const DeviceInfo &info, int threads, size_t smem, int *grid) {
     int per_sm = 0;
-    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS>, PROBE_THREADS, smem));
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS>, threads, smem));
     if (per_sm < 1) per_sm = 1;
     *grid = info.sms * per_sm;
     return VJ_OK;
@@ -210,6 +222,7 @@ struct JoinRun {
     // probe inputs prepared by the partition passes
     ProbeParams probe;
     bool aos;          // probe reads row-contiguous partition buffers
+    int threads;       // probe block size
     size_t probe_smem;
     int probe_grid;
 };
@@ -217,9 +230,10 @@ struct JoinRun {
 template <int KW, int PB, int HS, bool AOS>
 int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     run->aos = AOS;
+    run->threads = pl.threads;
     run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
     VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS>, run->probe_smem));
-    return probe_grid<KW, PB, HS, AOS>(ctx->info, run->probe_smem, &run->probe_grid);
+    return probe_grid<KW, PB, HS, AOS>(ctx->info, pl.threads, run->probe_smem, &run->probe_grid);
 }
 
 // Everything up to (not including) the probe launch. Returns probe parameters whose
@@ -234,7 +248,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
     const uint64_t item_cap = (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
-    auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint32_t **item_part, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
+    auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint4 **item_desc, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
         for (int pass = 0; pass < 2; pass++) {
             for (int sd = 0; sd < 2; sd++) {
                 bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
@@ -243,22 +257,23 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, pl.max_units[0]);
         if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, pl.max_units[1]);
         *item_begin = c.take<uint32_t>((size_t)np + 2);
-        *item_part = c.take<uint32_t>(item_cap);
+        *item_desc = c.take<uint4>(item_cap);
         *ticket = c.take<uint32_t>(1);
         *out_count = c.take<unsigned long long>(1);
         *error = c.take<uint32_t>(1);
     };
     void *bufs[2][2];
     PassBufs pb0{}, pb1{};
-    uint32_t *item_begin, *item_part, *ticket, *error;
+    uint32_t *item_begin, *ticket, *error;
+    uint4 *item_desc;
     unsigned long long *out_count;
     Carver dry;
-    layout(dry, bufs, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
+    layout(dry, bufs, &pb0, &pb1, &item_begin, &item_desc, &ticket, &out_count, &error);
     void *ws = nullptr;
     VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
     Carver c;
     c.base = (char *)ws;
-    layout(c, bufs, &pb0, &pb1, &item_begin, &item_part, &ticket, &out_count, &error);
+    layout(c, bufs, &pb0, &pb1, &item_begin, &item_desc, &ticket, &out_count, &error);
     VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
     ctx->launches = 0;
 
@@ -325,7 +340,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     // slot bits: the 14 bits right below the partition bits (tables hold at most 2^14 slots)
     Pq.slot_shift = 64 - (pl.bits[0] + pl.bits[1]) - 14;
     Pq.item_begin = item_begin;
-    Pq.item_part = item_part;
+    Pq.item_desc = item_desc;
     Pq.item_cap = (uint32_t)(item_cap < 0xffffffffull ? item_cap : 0xffffffffull);
     Pq.ticket = ticket;
     Pq.out_count = out_count;
@@ -346,9 +361,9 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
     plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
     VJ_CUDA(cudaGetLastError());
     if (run.aos) {
-        probe_kernel<KW, PB, HS, true><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+        probe_kernel<KW, PB, HS, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     } else {
-        probe_kernel<KW, PB, HS, false><<<run.probe_grid, PROBE_THREADS, run.probe_smem, stream>>>(run.probe);
+        probe_kernel<KW, PB, HS, false><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     }
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_PROBE_END, stream);

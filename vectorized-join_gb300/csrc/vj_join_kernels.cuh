@@ -99,8 +99,8 @@ struct ProbeParams {
     uint32_t rcap;         // build rows per item (a power of two; table capacity <= 2*rcap)
     uint32_t schunk;       // probe rows per item
     uint32_t outcap;       // staged output pairs per block
-    uint32_t *item_begin;  // [np+2]: prefix, total, and whether item_part is filled
-    uint32_t *item_part;   // [item_cap]: partition of each item
+    uint32_t *item_begin;  // [np+2]: prefix, total, and whether item_desc is filled
+    uint4 *item_desc;      // [item_cap]: build rows [x, y), probe rows [z, w) of each item
     uint32_t item_cap;
     uint32_t sub_rows;     // probe rows per bulk copy
     int slot_shift;        // table slot = (mix_hash(hash) >> slot_shift) & (capacity - 1)
@@ -296,6 +296,24 @@ struct Chunk {
         }
     }
 
+    // Ask L2 for rows [a, b) ahead of their bulk copy. Called by one thread.
+    __device__ __forceinline__ static void prefetch(const void *keys, const void *pay, const void *hash, const void *rows, uint32_t a, uint32_t b) {
+        if (a >= b) return;
+        if (AOS) {
+            const ColWindow w = col_window(rows, L::STRIDE, a, b);
+            bulk_prefetch_l2(w.src, w.bytes);
+        } else {
+            const ColWindow wk = col_window(keys, L::KB, a, b);
+            const ColWindow wp = col_window(pay, PB, a, b);
+            bulk_prefetch_l2(wk.src, wk.bytes);
+            bulk_prefetch_l2(wp.src, wp.bytes);
+            if (HS) {
+                const ColWindow wh = col_window(hash, HS, a, b);
+                bulk_prefetch_l2(wh.src, wh.bytes);
+            }
+        }
+    }
+
     __device__ __forceinline__ static Chunk view(const unsigned char *buf, uint32_t cap, const uint32_t *deltas) {
         Chunk c;
         if (AOS) {
@@ -358,6 +376,15 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_units_kernel(PassParams P) 
     }
 }
 
+// L2 prefetch of what the histogram reads of rows [a, b): the hash or key column, or the rows.
+template <int KW, int PB, int HS, bool AOS>
+__device__ __forceinline__ void histogram_prefetch(const Side &S, uint32_t a, uint32_t b) {
+    using L = Layout<KW, PB, HS>;
+    if (a >= b) return;
+    const ColWindow w = AOS ? col_window(S.rows_in, L::STRIDE, a, b) : (HS ? col_window(S.hash_in, HS, a, b) : col_window(S.keys_in, L::KB, a, b));
+    bulk_prefetch_l2(w.src, w.bytes);
+}
+
 // Hash of row i read straight from global memory (histogram pass).
 template <int KW, int PB, int HS, bool AOS>
 __device__ __forceinline__ uint64_t global_row_hash(const Side &S, uint32_t i, const HashSpec &hs) {
@@ -396,8 +423,16 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
     __syncthreads();
     constexpr int UNROLL = 4;
+    constexpr uint32_t STEP = UNROLL * PART_THREADS;
+    // keep the next AHEAD steps of this unit on their way to L2
+    constexpr uint32_t AHEAD = 4;
+    if (threadIdx.x == 0) histogram_prefetch<KW, PB, HS, AOS>(S, U.y, min(U.z, U.y + AHEAD * STEP));
     uint32_t i = U.y + threadIdx.x;
     for (; i + (UNROLL - 1) * PART_THREADS < U.z; i += UNROLL * PART_THREADS) {
+        if (threadIdx.x == 0) {
+            const uint32_t pa = i + AHEAD * STEP;
+            if (pa < U.z) histogram_prefetch<KW, PB, HS, AOS>(S, pa, min(U.z, pa + STEP));
+        }
         uint64_t h[UNROLL];
 #pragma unroll
         for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * PART_THREADS, P.hs);
@@ -519,10 +554,19 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         }
     }
 
+    if (threadIdx.x == 0 && ntiles > 2) {
+        const uint32_t a = U.y + 2 * T;
+        C::prefetch(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T));
+    }
     for (uint32_t k = 0; k < ntiles; k++) {
         const uint32_t buf = k & 1;
         const uint32_t tile = U.y + k * T;
         const uint32_t nt = min(U.z - tile, (uint32_t)T);
+        if (threadIdx.x == 0 && k + 3 < ntiles) {
+            // tile k + 2 is copied once tile k is sorted; have L2 fetch tile k + 3 already
+            const uint32_t a = U.y + (k + 3) * T;
+            C::prefetch(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T));
+        }
         for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_cnt[b] = 0;
         if (!block_wait(&bar[buf], (k >> 1) & 1)) {
             if (threadIdx.x == 0) {
@@ -623,10 +667,17 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q)
     for (int p = p0; p < p0 + per && p < Q.np; p++) {
         Q.item_begin[p] = too_many ? 0u : (uint32_t)run;
         const unsigned long long n = items_of(Q, p);
-        if (fill) {
-            for (unsigned long long k = 0; k < n; k++) Q.item_part[run + k] = (uint32_t)p;
+        if (fill && n) {
+            const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
+            const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
+            for (uint32_t r0 = rb; r0 < re; r0 += Q.rcap) {
+                for (uint32_t s0 = sb; s0 < se; s0 += Q.schunk) {
+                    Q.item_desc[run++] = make_uint4(r0, min(re, r0 + Q.rcap), s0, min(se, s0 + Q.schunk));
+                }
+            }
+        } else {
+            run += n;
         }
-        run += n;
     }
     if (threadIdx.x == 0) {
         Q.item_begin[Q.np] = too_many ? 0u : (uint32_t)total;
@@ -651,27 +702,61 @@ struct Pair<8> {
 };
 
 // Shared memory of the probe kernel: barriers, the build chunk as copied, the table of
-// build-row indices, two probe sub-chunks and the output staging area.
+// build-row indices (16-bit), two probe sub-chunks and two output staging buffers of
+// `outcap` pairs.
 template <int KW, int PB, int HS, bool AOS>
 struct ProbeSmem {
     using C = Chunk<KW, PB, HS, AOS>;
     __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t sub, uint32_t outcap) {
-        return 32 + C::bytes(rcap) + (size_t)tcap * 4 + 2 * C::bytes(sub) + (size_t)outcap * 2 * PB;
+        return 32 + C::bytes(rcap) + ((size_t)tcap * 2 + 15) / 16 * 16 + 2 * C::bytes(sub) + 2 * (size_t)outcap * 2 * PB;
     }
 };
 
-// Write the staged pairs [0, n) to the output at a block of positions taken from the
-// global counter; positions at or past the capacity are dropped (the count still grows).
-template <int PB>
-__device__ __forceinline__ void flush_pairs(const ProbeParams &Q, typename Pair<PB>::T *stage, uint32_t n, unsigned long long *s_base) {
-    using PT = typename Pair<PB>::T;
-    if (threadIdx.x == 0) *s_base = atomicAdd(Q.out_count, (unsigned long long)n);
-    __syncthreads();
-    const unsigned long long base = *s_base;
-    PT *out = (PT *)Q.out;
-    for (uint32_t i = threadIdx.x; i < n; i += PROBE_THREADS) {
-        if (base + i < Q.capacity) __stcs(out + base + i, stage[i]);
+// Rows of work item `it`: build rows [x, y), probe rows [z, w) -- from the planner's
+// descriptor, or (plans too large for the descriptor array) from a search of the prefix.
+__device__ __forceinline__ uint4 item_rows(const ProbeParams &Q, uint32_t it, bool direct) {
+    if (direct) return Q.item_desc[it];
+    int lo = 0, hi = Q.np - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (Q.item_begin[mid] <= it) lo = mid;
+        else hi = mid - 1;
     }
+    const uint32_t p = (uint32_t)lo;
+    const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
+    const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
+    const uint32_t nsc = (se - sb + Q.schunk - 1) / Q.schunk;
+    const uint32_t k = it - Q.item_begin[p];
+    const uint32_t r0 = rb + (k / nsc) * Q.rcap;
+    const uint32_t s0 = sb + (k % nsc) * Q.schunk;
+    return make_uint4(r0, min(re, r0 + Q.rcap), s0, min(se, s0 + Q.schunk));
+}
+
+// End of a probe sub-chunk (all threads): reserve the output range of the buffer just
+// filled (one atomic, whose result is read one sub-chunk later), copy out the buffer
+// filled before it, and switch buffers. The atomic's latency overlaps a sub-chunk of work.
+template <int PB>
+__device__ __forceinline__ void rotate_stage(const ProbeParams &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
+                                             unsigned long long *pend_base) {
+    using PT = typename Pair<PB>::T;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *flush_base = *pend_base;
+        *flush_n = *pend_n;
+        const uint32_t n = min(*out_n, Q.outcap);
+        *pend_n = n;
+        if (n) *pend_base = atomicAdd(Q.out_count, (unsigned long long)n);
+        *out_n = 0;
+    }
+    __syncthreads();
+    const uint32_t n = *flush_n;
+    const unsigned long long base = *flush_base;
+    const PT *src = stage0 + (size_t)(cur ^ 1) * Q.outcap;
+    PT *out = (PT *)Q.out;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        if (base + i < Q.capacity) __stcs(out + base + i, src[i]);
+    }
+    cur ^= 1;
 }
 
 template <int KW, int PB, int HS, bool AOS>
@@ -681,29 +766,47 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
     using PT = typename Pair<PB>::T;
     extern __shared__ __align__(16) unsigned char s_raw[];
     const uint32_t tcap_max = 2 * Q.rcap;  // rcap is a power of two
-    // layout: barriers | build chunk | table | probe sub-chunks x2 | output staging
+    // layout: barriers | build chunk | table | probe sub-chunks x2 | output staging x2
     uint64_t *bar = (uint64_t *)s_raw;  // [0] build chunk, [1], [2] probe sub-chunks
     unsigned char *rbuf = s_raw + 32;
-    uint32_t *t_idx = (uint32_t *)(rbuf + C::bytes(Q.rcap));
-    unsigned char *sbuf0 = (unsigned char *)(t_idx + tcap_max);
+    uint16_t *t_idx = (uint16_t *)(rbuf + C::bytes(Q.rcap));  // build row + 1, 0 = empty
+    unsigned char *sbuf0 = (unsigned char *)t_idx + ((size_t)tcap_max * 2 + 15) / 16 * 16;
     const size_t sbytes = C::bytes(Q.sub_rows);
-    PT *stage = (PT *)(sbuf0 + 2 * sbytes);
+    PT *stage0 = (PT *)(sbuf0 + 2 * sbytes);
 
-    __shared__ uint32_t s_item, s_part;
-    __shared__ uint32_t s_out_n;
-    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_item, s_next_item;
+    __shared__ uint4 s_rows, s_next_rows;
+    __shared__ uint32_t s_out_n;                 // pairs staged in the current buffer
+    __shared__ uint32_t s_flush_n;               // pairs of the other buffer awaiting copy-out
+    __shared__ unsigned long long s_flush_base;  // their output position
     __shared__ uint32_t s_rdelta[3];
     __shared__ uint32_t s_sdelta[2][3];
     __shared__ int s_dups;
     const int lane = threadIdx.x & 31;
     const uint32_t total_items = Q.item_begin[Q.np];
     const bool direct = Q.item_begin[Q.np + 1] != 0;
+    // Output: sub-chunk k stages into buffer k & 1. At its end thread 0 reserves its output
+    // range with one atomic, whose result is only read at the end of sub-chunk k + 1, when
+    // the buffer is copied out -- the atomic's latency overlaps a sub-chunk of probing.
+    __shared__ unsigned long long s_pend_base;  // reservation of the buffer not yet copied
+    __shared__ uint32_t s_pend_n;
+    uint32_t cur = 0;                           // staging buffer being filled (uniform)
     if (threadIdx.x == 0) {
         s_out_n = 0;
+        s_flush_n = 0;
+        s_pend_base = 0;
+        s_pend_n = 0;
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_init(&bar[2], 1);
         fence_proxy_async();
+        s_next_item = atomicAdd(Q.ticket, 1u);
+        if (s_next_item < total_items) {
+            const uint4 d = item_rows(Q, s_next_item, direct);
+            s_next_rows = d;
+            C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
+            C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
+        }
     }
     uint32_t r_loads = 0;   // build-chunk copies waited for so far (parity of bar[0])
     uint32_t s_issued = 0;  // probe sub-chunk copies issued / waited for
@@ -712,37 +815,24 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            const uint32_t it = atomicAdd(Q.ticket, 1u);
-            uint32_t p = 0;
-            if (it < total_items) {
-                if (direct) {
-                    p = Q.item_part[it];
-                } else {
-                    int lo = 0, hi = Q.np - 1;
-                    while (lo < hi) {
-                        int mid = (lo + hi + 1) >> 1;
-                        if (Q.item_begin[mid] <= it) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    p = (uint32_t)lo;
+            s_item = s_next_item;
+            s_rows = s_next_rows;
+            s_dups = 0;
+            if (s_item < total_items) {
+                s_next_item = atomicAdd(Q.ticket, 1u);
+                if (s_next_item < total_items) {
+                    const uint4 d = item_rows(Q, s_next_item, direct);
+                    s_next_rows = d;
+                    C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
+                    C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
                 }
             }
-            s_item = it;
-            s_part = p;
-            s_dups = 0;
         }
         __syncthreads();
         const uint32_t item = s_item;
         if (item >= total_items) break;
-        const uint32_t p = s_part;
-        const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
-        const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
-        const uint32_t nsc = (se - sb + Q.schunk - 1) / Q.schunk;
-        const uint32_t k = item - Q.item_begin[p];
-        const uint32_t r0 = rb + (k / nsc) * Q.rcap;
-        const uint32_t r1 = min(re, r0 + Q.rcap);
-        const uint32_t s0 = sb + (k % nsc) * Q.schunk;
-        const uint32_t s1 = min(se, s0 + Q.schunk);
+        const uint4 d = s_rows;
+        const uint32_t r0 = d.x, r1 = d.y, s0 = d.z, s1 = d.w;
         const uint32_t nr = r1 - r0;
         const uint32_t nsub = (s1 - s0 + Q.sub_rows - 1) / Q.sub_rows;
         uint32_t cap = 64;
@@ -756,7 +846,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
             C::issue(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, s0, min(s1, s0 + Q.sub_rows), Q.sub_rows, sbuf0 + sbi * sbytes, &bar[1 + sbi], s_sdelta[sbi]);
         }
         s_issued++;
-        for (uint32_t i = threadIdx.x; i < cap; i += PROBE_THREADS) t_idx[i] = 0;
+        for (uint32_t i = threadIdx.x; i < cap / 8; i += blockDim.x) ((uint4 *)t_idx)[i] = make_uint4(0, 0, 0, 0);
         const bool ok_r = block_wait(&bar[0], r_loads & 1);
         r_loads++;
         if (!ok_r) {
@@ -769,14 +859,14 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         // ---- build: table of build-row indices (+1) keyed by the mixed hash; an equal key
         // met on the way marks the chunk as having duplicate keys
         const C R = C::view(rbuf, Q.rcap, s_rdelta);
-        for (uint32_t i = threadIdx.x; i < nr; i += PROBE_THREADS) {
+        for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) {
             const Key<KW> key = R.key(i);
             const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
             uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
             uint32_t tries = 0;
             bool dup = false;
             for (;;) {
-                const uint32_t prev = atomicCAS(&t_idx[slot], 0u, i + 1);
+                const uint32_t prev = atomicCAS(&t_idx[slot], (unsigned short)0, (unsigned short)(i + 1));
                 if (prev == 0u) break;
                 dup |= key_equal<KW>(R.key(prev - 1), key);
                 slot = (slot + 1) & cmask;
@@ -809,73 +899,141 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                 s_issued++;
             }
             const C Sv = C::view(sbuf0 + sbi * sbytes, Q.sub_rows, s_sdelta[sbi]);
+            PT *stage = stage0 + (size_t)cur * Q.outcap;
             const uint32_t a = s0 + sub * Q.sub_rows;
             const uint32_t ns = min(s1 - a, Q.sub_rows);
-            for (uint32_t base = 0; base < ns; base += PROBE_THREADS) {
-                const uint32_t i = base + threadIdx.x;
-                bool active = i < ns;
-                Key<KW> skey;
-                uint64_t sh = 0;
-                uint32_t slot = 0;
-                if (active) {
-                    skey = Sv.key(i);
-                    sh = HS ? Sv.hash(i) : row_hash<KW>(skey, Q.hs);
-                    slot = (uint32_t)(mix_hash(sh) >> Q.slot_shift) & cmask;
-                }
-                // Lanes walk their probe sequences in lock step; each step emits the lanes
-                // that matched with one shared-memory reservation per warp. Without
-                // duplicate build keys a probe row stops at its first match.
-                while (__any_sync(0xffffffffu, active)) {
-                    bool match = false;
-                    Pt rp = 0;
-                    if (active) {
-                        const uint32_t e = t_idx[slot];
-                        if (e == 0) {
-                            active = false;
-                        } else {
-                            if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.hash(e - 1) == sh)) {
-                                match = true;
-                                rp = R.pay(e - 1);
-                                active = dups;
-                            }
-                            slot = (slot + 1) & cmask;
-                        }
+            if (!dups) {
+                // Unique build keys: a probe row has at most one match. Each thread resolves
+                // two rows on its own, then the warp emits its matches with one reservation.
+                for (uint32_t base = 0; base < ns; base += 2 * blockDim.x) {
+                    const uint32_t i0 = base + threadIdx.x, i1 = i0 + blockDim.x;
+                    bool a0 = i0 < ns, a1 = i1 < ns;
+                    Key<KW> k0, k1;
+                    uint64_t h0 = 0, h1 = 0;
+                    uint32_t sl0 = 0, sl1 = 0;
+                    if (a0) {
+                        k0 = Sv.key(i0);
+                        h0 = HS ? Sv.hash(i0) : row_hash<KW>(k0, Q.hs);
+                        sl0 = (uint32_t)(mix_hash(h0) >> Q.slot_shift) & cmask;
                     }
-                    const uint32_t m = __ballot_sync(0xffffffffu, match);
-                    if (m) {
-                        const int leader = __ffs(m) - 1;
-                        uint32_t pos0 = 0;
-                        if (lane == leader) pos0 = atomicAdd(&s_out_n, (uint32_t)__popc(m));
-                        pos0 = __shfl_sync(0xffffffffu, pos0, leader);
-                        if (match) {
-                            const uint32_t pos = pos0 + __popc(m & lanemask_lt());
-                            const Pt sp = Sv.pay(i);
-                            if (pos < Q.outcap) {
-                                stage[pos] = Pair<PB>::make(rp, sp);
+                    if (a1) {
+                        k1 = Sv.key(i1);
+                        h1 = HS ? Sv.hash(i1) : row_hash<KW>(k1, Q.hs);
+                        sl1 = (uint32_t)(mix_hash(h1) >> Q.slot_shift) & cmask;
+                    }
+                    int m0 = -1, m1 = -1;
+                    while (a0 | a1) {
+                        if (a0) {
+                            const uint32_t e = t_idx[sl0];
+                            if (e == 0) {
+                                a0 = false;
+                            } else if (key_equal<KW>(R.key(e - 1), k0) && (!HS || R.hash(e - 1) == h0)) {
+                                m0 = (int)e - 1;
+                                a0 = false;
                             } else {
-                                // staging full (build rows with many duplicates): direct write
+                                sl0 = (sl0 + 1) & cmask;
+                            }
+                        }
+                        if (a1) {
+                            const uint32_t e = t_idx[sl1];
+                            if (e == 0) {
+                                a1 = false;
+                            } else if (key_equal<KW>(R.key(e - 1), k1) && (!HS || R.hash(e - 1) == h1)) {
+                                m1 = (int)e - 1;
+                                a1 = false;
+                            } else {
+                                sl1 = (sl1 + 1) & cmask;
+                            }
+                        }
+                    }
+                    const uint32_t b0 = __ballot_sync(0xffffffffu, m0 >= 0);
+                    const uint32_t b1 = __ballot_sync(0xffffffffu, m1 >= 0);
+                    const uint32_t total = __popc(b0) + __popc(b1);
+                    if (total) {
+                        uint32_t pos0 = 0;
+                        if (lane == 0) pos0 = atomicAdd(&s_out_n, total);
+                        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+                        const uint32_t lt = lanemask_lt();
+                        if (m0 >= 0) {
+                            const uint32_t pos = pos0 + __popc(b0 & lt);
+                            const PT pr = Pair<PB>::make(R.pay((uint32_t)m0), Sv.pay(i0));
+                            if (pos < Q.outcap) {
+                                stage[pos] = pr;
+                            } else {
                                 const unsigned long long g = atomicAdd(Q.out_count, 1ull);
-                                if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, sp);
+                                if (g < Q.capacity) ((PT *)Q.out)[g] = pr;
+                            }
+                        }
+                        if (m1 >= 0) {
+                            const uint32_t pos = pos0 + __popc(b0) + __popc(b1 & lt);
+                            const PT pr = Pair<PB>::make(R.pay((uint32_t)m1), Sv.pay(i1));
+                            if (pos < Q.outcap) {
+                                stage[pos] = pr;
+                            } else {
+                                const unsigned long long g = atomicAdd(Q.out_count, 1ull);
+                                if (g < Q.capacity) ((PT *)Q.out)[g] = pr;
+                            }
+                        }
+                    }
+                }
+            } else {
+                for (uint32_t base = 0; base < ns; base += blockDim.x) {
+                    const uint32_t i = base + threadIdx.x;
+                    bool active = i < ns;
+                    Key<KW> skey;
+                    uint64_t sh = 0;
+                    uint32_t slot = 0;
+                    if (active) {
+                        skey = Sv.key(i);
+                        sh = HS ? Sv.hash(i) : row_hash<KW>(skey, Q.hs);
+                        slot = (uint32_t)(mix_hash(sh) >> Q.slot_shift) & cmask;
+                    }
+                    // Lanes walk their probe sequences in lock step; each step emits the lanes
+                    // that matched with one shared-memory reservation per warp. Without
+                    // duplicate build keys a probe row stops at its first match.
+                    while (__any_sync(0xffffffffu, active)) {
+                        bool match = false;
+                        Pt rp = 0;
+                        if (active) {
+                            const uint32_t e = t_idx[slot];
+                            if (e == 0) {
+                                active = false;
+                            } else {
+                                if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.hash(e - 1) == sh)) {
+                                    match = true;
+                                    rp = R.pay(e - 1);
+                                    active = dups;
+                                }
+                                slot = (slot + 1) & cmask;
+                            }
+                        }
+                        const uint32_t m = __ballot_sync(0xffffffffu, match);
+                        if (m) {
+                            const int leader = __ffs(m) - 1;
+                            uint32_t pos0 = 0;
+                            if (lane == leader) pos0 = atomicAdd(&s_out_n, (uint32_t)__popc(m));
+                            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+                            if (match) {
+                                const uint32_t pos = pos0 + __popc(m & lanemask_lt());
+                                const Pt sp = Sv.pay(i);
+                                if (pos < Q.outcap) {
+                                    stage[pos] = Pair<PB>::make(rp, sp);
+                                } else {
+                                    // staging full (build rows with many duplicates): direct write
+                                    const unsigned long long g = atomicAdd(Q.out_count, 1ull);
+                                    if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, sp);
+                                }
                             }
                         }
                     }
                 }
             }
-            __syncthreads();
-            uint32_t n = s_out_n;
-            if (n > Q.outcap) n = Q.outcap;
-            if (n + Q.sub_rows > Q.outcap) {
-                flush_pairs<PB>(Q, stage, n, &s_base);
-                __syncthreads();
-                if (threadIdx.x == 0) s_out_n = 0;
-                __syncthreads();
-            }
+            rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
         }
     }
-    __syncthreads();
-    uint32_t n = s_out_n;
-    if (n > Q.outcap) n = Q.outcap;
-    if (n) flush_pairs<PB>(Q, stage, n, &s_base);
+    // drain: the buffer filled last and the one before it
+    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
+    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
 }
 
 }  // namespace vj

@@ -82,7 +82,9 @@ class VjJoinOptions(ctypes.Structure):
         ("radix_bits", ctypes.c_int32 * 2),
         ("build_rows", ctypes.c_int32),
         ("probe_rows", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("probe_threads", ctypes.c_int32),
+        ("probe_sub_rows", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -254,7 +256,7 @@ def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTa
     return t
 
 
-def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0) -> VjJoinOptions:
+def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, probe_sub_rows: int = 0) -> VjJoinOptions:
     o = VjJoinOptions()
     o.hash_algo = hash_algo
     o.hash_bits = hash_bits
@@ -265,6 +267,8 @@ def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, r
     o.radix_bits[1] = radix_bits[1]
     o.build_rows = build_rows
     o.probe_rows = probe_rows
+    o.probe_threads = probe_threads
+    o.probe_sub_rows = probe_sub_rows
     return o
 
 
