@@ -162,6 +162,33 @@ VJ_API int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashes_in
                  uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream);
 
 /*
+ * vj_partition_noalloc -- vj_partition without a context, and without allocating anything.
+ * It has no counterpart in the reference (whose partition_gpu allocates its buffers on every
+ * call). It is meant for callers that cannot allocate device memory: an engine that has
+ * handed all of HBM to its own buffer pool, so that cudaMalloc fails or would compete with
+ * it, or one that keeps other streams busy and cannot let a cudaFree synchronise the device.
+ *
+ * Arguments, bucket rule, outputs and errors are those of vj_partition. The caller passes
+ * every input and output; the working memory of the pass (per-unit bucket counts and
+ * offsets, bucket bounds, an error flag) is one static device array of
+ * VJ_NOALLOC_SCRATCH_BYTES that each GPU which loads the library holds until the process
+ * exits. The call runs no cudaMalloc, cudaFree or other allocating routine.
+ *   - radix_bits: 1..VJ_NOALLOC_MAX_RADIX_BITS; larger values return VJ_ERR_UNSUPPORTED
+ *     before anything is launched.
+ *   - It runs on the calling thread's current device. The first call on each device looks
+ *     up the device address of the static array (cudaGetSymbolAddress) and keeps it; make
+ *     that first call before any stream capture.
+ *   - Every call on a device shares the one array, which keeps what the last call left in
+ *     it; each call clears what must start at zero itself. Calls that overlap on the GPU
+ *     (streams with no order between them, or threads without a lock) race on the array and
+ *     give wrong results: put them on one stream or serialise them.
+ */
+#define VJ_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define VJ_NOALLOC_MAX_RADIX_BITS 10
+VJ_API int vj_partition_noalloc(const vj_table *in, const void *d_hashes_in, int hash_bits, int hash_algo, void *d_keys_out, void *d_payloads_out, void *d_hashes_out, int radix_shift, int radix_bits,
+                         uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream);
+
+/*
  * vj_build_probe -- build_and_probe_gpu (src/join/join_provider.cu:669-847).
  * Builds a hash table over r and probes it with s; a match is a pair of rows with equal
  * hashes (when hash arrays are given) and equal key words. Writes up to `capacity` pairs

@@ -822,3 +822,174 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     }
     return status;
 }
+
+// ------------------------------------------------------------------ vj_partition_noalloc
+//
+// A radix pass for callers that cannot allocate device memory (an engine whose own pool
+// holds all of HBM, or one that cannot let cudaFree synchronise a device its other streams
+// are using). The pass's working memory lives in the static array below instead of a
+// context workspace; everything else is the vj_partition sequence.
+
+// Working memory of vj_partition_noalloc, one copy per device that loads the library. In
+// host code this name stands for a host-side shadow, not for device memory: host code
+// passes kernels the address cudaGetSymbolAddress returns for the current device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VJ_NOALLOC_SCRATCH_BYTES];
+
+namespace vj {
+namespace {
+
+std::mutex g_noalloc_mutex;
+char *g_noalloc_base[64];
+
+// Device address of the scratch on `device` (the current device), looked up on the first
+// call for that device and kept for the life of the process.
+int noalloc_scratch(int device, char **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            return cuda_error(e, "vj_partition_noalloc: device address of the static scratch");
+        }
+        g_noalloc_base[device] = (char *)p;
+    }
+    *out = g_noalloc_base[device];
+    return VJ_OK;
+}
+
+struct NoallocLayout {
+    PassBufs pb;
+    unsigned long long *hist, *off;
+    uint32_t *err;
+};
+
+NoallocLayout noalloc_layout(Carver &c, int bins, int units) {
+    NoallocLayout L;
+    L.pb = carve_pass(c, 1, bins, units);
+    L.hist = c.take<unsigned long long>(bins);
+    L.off = c.take<unsigned long long>(bins);
+    L.err = c.take<uint32_t>(1);
+    return L;
+}
+
+// Work units of the pass: as many as vj_partition uses (16 per SM), fewer when their
+// bucket counts and offsets (8 bytes per bucket per unit) would not fit in the scratch.
+// 0: not even two units fit.
+int noalloc_units(int sms, int bins) {
+    Carver fixed;
+    noalloc_layout(fixed, bins, 0);
+    const size_t per_unit = sizeof(uint4) + 2 * sizeof(uint32_t) * (size_t)bins;
+    const size_t slack = 3 * 256;  // alignment of the three per-unit arrays
+    const size_t room = VJ_NOALLOC_SCRATCH_BYTES > fixed.off + slack ? VJ_NOALLOC_SCRATCH_BYTES - fixed.off - slack : 0;
+    size_t units = room / per_unit;
+    if (units > (size_t)sms * 16 + 1) units = (size_t)sms * 16 + 1;
+    Carver check;
+    noalloc_layout(check, bins, (int)units);
+    return units >= 2 && check.off <= VJ_NOALLOC_SCRATCH_BYTES ? (int)units : 0;
+}
+
+template <int KW, int PB, int HS>
+int partition_noalloc_typed(char *scratch, int units, const vj_table *in, const void *hashes_in, const HashSpec &hs, void *keys_out, void *pay_out, void *hash_out, int shift, int bits, uint64_t *d_hist,
+                            uint64_t *d_off, uint64_t *h_hist, uint64_t *h_off, cudaStream_t stream) {
+    const int bins = 1 << bits;
+    Carver c;
+    c.base = scratch;
+    const NoallocLayout L = noalloc_layout(c, bins, units);
+    // The scratch holds whatever the previous call left. The error flag must start at zero;
+    // the pass clears its own bucket totals and overwrites every other array before use.
+    VJ_CUDA(cudaMemsetAsync(L.err, 0, sizeof(uint32_t), stream));
+    PassParams P{};
+    P.side[0].keys_in = in->keys;
+    P.side[0].pay_in = in->payloads;
+    P.side[0].hash_in = hashes_in;
+    P.side[0].rows_in = nullptr;
+    P.side[0].rows_out = nullptr;
+    P.side[0].keys_out = keys_out;
+    P.side[0].pay_out = pay_out;
+    P.side[0].hash_out = hash_out;
+    P.side[0].rows = (uint32_t)in->rows;
+    P.nsides = 1;
+    P.Q = 1;
+    P.seg_begin = P.seg_end = nullptr;
+    P.shift = shift;
+    P.bits = bits;
+    P.hs = hs;
+    P.max_units = units;
+    P.min_unit_rows = 4096;
+    P.error = L.err;
+    if (in->rows > 0) {
+        VJ_TRY((run_pass<KW, PB, HS, false, false>(nullptr, 0, P, L.pb, stream)));
+    } else {
+        VJ_CUDA(cudaMemsetAsync(L.pb.part_begin, 0, bins * sizeof(uint32_t), stream));
+        VJ_CUDA(cudaMemsetAsync(L.pb.part_end, 0, bins * sizeof(uint32_t), stream));
+    }
+    unsigned long long *hist = d_hist ? (unsigned long long *)d_hist : L.hist;
+    unsigned long long *off = d_off ? (unsigned long long *)d_off : L.off;
+    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(L.pb.part_begin, L.pb.part_end, bins, hist, off);
+    VJ_CUDA(cudaGetLastError());
+    if (h_hist || h_off) {
+        if (h_hist) VJ_CUDA(cudaMemcpyAsync(h_hist, hist, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+        if (h_off) VJ_CUDA(cudaMemcpyAsync(h_off, off, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+        uint32_t herr = 0;
+        VJ_CUDA(cudaMemcpyAsync(&herr, L.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        VJ_CUDA(cudaStreamSynchronize(stream));
+        VJ_CHECK(herr == 0, VJ_ERR_DEVICE, "vj_partition_noalloc: a kernel reported an internal limit (flags %x)", herr);
+    }
+    return VJ_OK;
+}
+
+struct NoallocPartitionCall {
+    char *scratch;
+    int units;
+    const vj_table *in;
+    const void *hashes;
+    HashSpec hs;
+    void *ko, *po, *ho;
+    int shift, bits;
+    uint64_t *dh, *doff, *hh, *hoff;
+    cudaStream_t stream;
+    template <int KW, int PB, int HS>
+    int run() {
+        return partition_noalloc_typed<KW, PB, HS>(scratch, units, in, hashes, hs, ko, po, ho, shift, bits, dh, doff, hh, hoff, stream);
+    }
+};
+
+}  // namespace
+}  // namespace vj
+
+extern "C" int vj_partition_noalloc(const vj_table *in, const void *d_hashes_in, int hash_bits, int hash_algo, void *d_keys_out, void *d_payloads_out, void *d_hashes_out, int radix_shift, int radix_bits,
+                                    uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream) {
+    // every argument is checked before the first CUDA call
+    VJ_TRY(check_table(in, "vj_partition_noalloc: in"));
+    VJ_CHECK(radix_bits >= 1 && radix_bits <= VJ_NOALLOC_MAX_RADIX_BITS, VJ_ERR_UNSUPPORTED,
+             "vj_partition_noalloc: radix_bits %d is outside [1, %d], the buckets its %u-byte static scratch holds (vj_partition takes up to %d)", radix_bits, VJ_NOALLOC_MAX_RADIX_BITS,
+             (unsigned)VJ_NOALLOC_SCRATCH_BYTES, MAX_RADIX_BITS);
+    VJ_CHECK(hash_bits == 32 || hash_bits == 64, VJ_ERR_INVALID_ARGUMENT, "vj_partition_noalloc: hash_bits must be 32 or 64");
+    VJ_CHECK(radix_shift >= 0 && radix_shift < 64, VJ_ERR_INVALID_ARGUMENT, "vj_partition_noalloc: radix_shift must be in [0, 63]");
+    VJ_CHECK(hash_algo >= 0 && hash_algo < VJ_HASH_COUNT, VJ_ERR_INVALID_ARGUMENT, "vj_partition_noalloc: unknown hash algorithm %d", hash_algo);
+    VJ_CHECK(in->rows == 0 || (d_keys_out && d_payloads_out), VJ_ERR_INVALID_ARGUMENT, "vj_partition_noalloc: null output column");
+    int device = 0;
+    VJ_CUDA(cudaGetDevice(&device));
+    DeviceInfo info;
+    VJ_TRY(device_info(device, &info));
+    NoallocPartitionCall call;
+    VJ_TRY(noalloc_scratch(device, &call.scratch));
+    call.units = noalloc_units(info.sms, 1 << radix_bits);
+    VJ_CHECK(call.units > 0, VJ_ERR_UNSUPPORTED, "vj_partition_noalloc: %d buckets do not fit the %u-byte static scratch", 1 << radix_bits, (unsigned)VJ_NOALLOC_SCRATCH_BYTES);
+    call.in = in;
+    call.hashes = d_hashes_in;
+    call.hs.algo = hash_algo;
+    call.hs.hash_bits = hash_bits;
+    call.hs.mix = 0;
+    call.ko = d_keys_out;
+    call.po = d_payloads_out;
+    call.ho = d_hashes_in ? d_hashes_out : nullptr;
+    call.shift = radix_shift;
+    call.bits = radix_bits;
+    call.dh = d_histogram;
+    call.doff = d_offsets;
+    call.hh = h_histogram;
+    call.hoff = h_offsets;
+    call.stream = (cudaStream_t)stream;
+    return dispatch(in->key_words, in->payload_bytes, d_hashes_in ? hash_bits / 8 : 0, call);
+}

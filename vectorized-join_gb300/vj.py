@@ -53,6 +53,7 @@ EXPORTS = [
     "vj_ctx_set_profiling",
     "vj_ctx_last_profile",
     "vj_partition",
+    "vj_partition_noalloc",
     "vj_build_probe",
     "vj_join",
     "vj_join_host",
@@ -175,6 +176,8 @@ def load() -> ctypes.CDLL:
         L.vj_ctx_last_profile.argtypes = [vp, ctypes.POINTER(VjProfile)]
         L.vj_partition.restype = i32
         L.vj_partition.argtypes = [vp, ctypes.POINTER(VjTable), vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp]
+        L.vj_partition_noalloc.restype = i32
+        L.vj_partition_noalloc.argtypes = [ctypes.POINTER(VjTable), vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp]
         L.vj_build_probe.restype = i32
         L.vj_build_probe.argtypes = [vp, ctypes.POINTER(VjTable), vp, ctypes.POINTER(VjTable), vp, i32, i32, vp, u64, ctypes.POINTER(u64), vp]
         L.vj_join.restype = i32
@@ -333,6 +336,16 @@ class Context:
                 self.handle, ctypes.byref(t), ptr(hashes_in), hash_bits, hash_algo, ptr(keys_out), ptr(pay_out), ptr(hashes_out), radix_shift, radix_bits, ptr(d_hist), ptr(d_off), ptr(h_hist), ptr(h_off), stream_handle(stream)
             )
         )
+
+
+def partition_noalloc(t: VjTable, keys_out, pay_out, radix_shift: int, radix_bits: int, hashes_in=None, hash_bits: int = 64, hash_algo: int = 0, hashes_out=None, d_hist=None, d_off=None, h_hist=None, h_off=None, stream=None) -> None:
+    """vj_partition_noalloc on the current device: Context.partition without a context, for
+    callers that cannot allocate device memory (its scratch is a static device array)."""
+    check(
+        load().vj_partition_noalloc(
+            ctypes.byref(t), ptr(hashes_in), hash_bits, hash_algo, ptr(keys_out), ptr(pay_out), ptr(hashes_out), radix_shift, radix_bits, ptr(d_hist), ptr(d_off), ptr(h_hist), ptr(h_off), stream_handle(stream)
+        )
+    )
 
 
 def hash(d_in, n: int, chunk_offset: int, element_chunks: int, chunk_bits: int, hash_bits: int, algo: int | str, d_out, stream=None) -> None:
