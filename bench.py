@@ -155,6 +155,23 @@ def cpu_baseline(oracle, small: bool, budget_s: float = 12.0) -> dict:
     }
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The largest `value` over all ranks (the slowest rank's time); `value` itself at N=1."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank_step: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return units_per_rank_step * steps * world / (max_ms / 1000.0)
+
+
 def run_reference(args, cfg) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -232,13 +249,9 @@ def run_e2e(args, ctx, vj, torch, stream, dev, world, rk, rp, sk, sp, nr, ns, m,
     ev1.record(stream)
     torch.cuda.synchronize()
     assert got == m
-    e2e_ms = ev0.elapsed_time(ev1)
-    te = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_ms = float(te.item())
+    e2e_ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     return {
-        "value": n * e_steps * world / (e2e_ms / 1000.0),
+        "value": job_rate(n, e_steps, world, e2e_ms),
         "unit": UNIT,
         "h2d_bytes_per_step": n * w,
         "d2h_bytes_per_step": m * 2 * w_p,
@@ -326,13 +339,10 @@ def main():
     torch.cuda.synchronize()
     clocks = sampler.stop()
     step_ms = [events[i].elapsed_time(events[i + 1]) for i in range(args.steps)]
-    total_ms = events[0].elapsed_time(events[-1])
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    total_ms = max_over_ranks(events[0].elapsed_time(events[-1]), dev)
     if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dist.barrier()
-    total_ms = float(t.item())
-    value = (nr + ns) * args.steps * world / (total_ms / 1000.0)
+    value = job_rate(nr + ns, args.steps, world, total_ms)
 
     # ---- roofline of the dominant kernel (stage events recorded by the library)
     peak, peak_src = measured_peak()
