@@ -21,6 +21,7 @@ from __future__ import annotations
 import argparse
 import importlib.util
 import json
+import re
 import os
 import statistics
 import subprocess
@@ -153,6 +154,16 @@ def cpu_baseline(oracle, small: bool, budget_s: float = 12.0) -> dict:
         "kind": "port",
         "sample": f"2^{lr} x 2^{ls} rows of the same int64 50%-match workload (1/{(1 << 27) // nr} of each side), {runs} joins, {t_total:.1f} s",
     }
+
+
+def profiled_traffic(kernel: str):
+    """`traffic-per-launch-at-full-size: <kernel> <bytes>` from the summaries in profiles/."""
+    pat = re.compile(r"^traffic-per-launch-at-full-size:\s+(\w+)\s+(\d+)\s*$", re.M)
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for name, val in pat.findall(f.read_text()):
+            if name == kernel:
+                return int(val)
+    return None
 
 
 def max_over_ranks(value: float, device) -> float:
@@ -372,13 +383,9 @@ def main():
     ms_per_launch = sum(x[0] for x in launches) / len(launches)
     bytes_per_launch = sum(x[1] for x in launches) / len(launches)
     achieved = bytes_per_launch / (ms_per_launch / 1000.0) / 1e9
-    traffic = None
-    tpath = ROOT / "profiles" / "traffic.json"
-    if tpath.exists():
-        try:
-            traffic = json.loads(tpath.read_text()).get(dom_kind)
-        except Exception:
-            traffic = None
+    # DRAM bytes per launch of this kernel from the committed ncu summary of the same build
+    # (captured at 1/8 size and scaled by rows); only the full-size workload has one
+    traffic = profiled_traffic(dom_kind) if args.shift == 0 and not args.small else None
     roofline = {
         "kernel": dom_kind,
         "bound": "hbm",
