@@ -127,7 +127,12 @@ typedef struct vj_profile {
     float ms_total;             /* first partition launch to the end of the probe */
     uint64_t rows[2];           /* |R|, |S| */
     uint64_t matches;
+    int32_t tables;             /* VJ_TABLES_SHARED or VJ_TABLES_L2: where build tables lived */
+    int32_t fallbacks;          /* L2-table joins redone with shared-memory tables (long
+                                   duplicate clusters) */
 } vj_profile;
+
+enum { VJ_TABLES_SHARED = 0, VJ_TABLES_L2 = 1 };
 
 VJ_API int vj_ctx_set_profiling(vj_ctx *ctx, int enabled);
 VJ_API int vj_ctx_last_profile(const vj_ctx *ctx, vj_profile *out);
@@ -203,7 +208,12 @@ VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes
 
 /* Join options (JoinConfig, src/join/join_provider.cuh:108-122). A zero-initialised struct
  * means "automatic": FNV-1a, 64-bit hash, passes, radix bits and table size from the tuner. */
-enum { VJ_JOIN_FIXED_PASSES = 1 };
+/* flags: VJ_JOIN_FIXED_PASSES takes passes and radix_bits as given; VJ_JOIN_SHARED_TABLES
+ * and VJ_JOIN_L2_TABLES pick where the build tables live: shared-memory tables per build
+ * chunk of <= 8192 rows after up to two radix passes (the default), or L2-resident tables
+ * per partition of ~2^17 build rows after one pass (radix_bits[0], when fixed, is that
+ * pass's width; build_rows caps the rows per table). */
+enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4 };
 typedef struct vj_join_options {
     int32_t hash_algo;      /* VJ_HASH_*: the hash the partitions are cut from */
     int32_t hash_bits;      /* 32 or 64; 0 = 64 */

@@ -227,6 +227,7 @@ def test_generator_matches_oracle(vjlib, cuda, oracle):
         assert vjlib.generate_join_expect(42, nr, ns, thr) == oracle.gen_join_expect(42, nr, ns, 0.5)
 
 
+@pytest.mark.parametrize("tables", ["auto", "shared", "l2"])
 @pytest.mark.parametrize(
     "name,kb,pb,nr,ns,ratio",
     [
@@ -234,8 +235,9 @@ def test_generator_matches_oracle(vjlib, cuda, oracle):
         ("int64 50% join 2^27 x 2^29", 8, 8, 1 << 27, 1 << 29, 0.5),
     ],
 )
-def test_full_size_count_and_digest(vjlib, ctx, cuda, name, kb, pb, nr, ns, ratio):
-    """Benchmark sizes: count and order-independent digest equal the generator's truth."""
+def test_full_size_count_and_digest(vjlib, ctx, cuda, name, kb, pb, nr, ns, ratio, tables):
+    """Benchmark sizes: count and order-independent digest equal the generator's truth,
+    with the planner's choice of tables and with each kind forced."""
     import torch
 
     thr = int(round(ratio * (1 << 32)))
@@ -249,8 +251,11 @@ def test_full_size_count_and_digest(vjlib, ctx, cuda, name, kb, pb, nr, ns, rati
     want = vjlib.generate_join_expect(42, nr, ns, thr)
     cap = want[0]
     out = torch.empty((cap, 2), dtype=pt, device=cuda)
-    res = ctx.join(vjlib.table(rk, rp, nr, kb // 4, pb), vjlib.table(sk, sp, ns, kb // 4, pb), out=out, capacity=cap)
+    opts = vjlib.options(tables=tables)
+    res = ctx.join(vjlib.table(rk, rp, nr, kb // 4, pb), vjlib.table(sk, sp, ns, kb // 4, pb), opts, out=out, capacity=cap)
     assert res.count == want[0], name
+    if tables != "auto":
+        assert ctx.last_profile().tables == (1 if tables == "l2" else 0)
     assert vjlib.pairs_digest(out, res.count, pb) == (want[1], want[2]), name
     del rk, sk, rp, sp, out
     torch.cuda.empty_cache()

@@ -7,7 +7,7 @@
 // buffer per pair (:694). Here one stream carries a fixed sequence of launches; every
 // decision that depends on data (unit split, partition bounds, work items) is made on
 // the device, and the host synchronises once, to read the match count.
-#include "vj_join_kernels.cuh"
+#include "vj_l2_kernels.cuh"
 
 #include <cstring>
 #include <mutex>
@@ -41,6 +41,16 @@ struct Plan {
     uint32_t outcap = 1536;   // staged output pairs per block
     int threads = PROBE_THREADS;  // probe block size
     int max_units[2] = {0, 0};
+    // where the build tables live; L2 tables follow one radix pass
+    int tables = VJ_TABLES_SHARED;
+    int fallbacks = 0;            // L2 plans that were redone with shared-memory tables
+    uint32_t l2_rc = 1u << 18;    // build rows per seq at most
+    uint32_t l2_region_slots = 0;
+    int l2_ring = 8;
+    int l2_lag = 2;
+    uint32_t l2_build_rows = 4096;
+    uint32_t l2_probe_rows = 8192;
+    uint32_t l2_outcap = 2048;
 };
 
 int ceil_log2(uint64_t x) {
@@ -56,8 +66,12 @@ size_t probe_smem_budget(const DeviceInfo &info) {
     return per_block < two ? per_block : two;
 }
 
+// Build rows per partition the L2-table plan aims at: its table (8-byte slots, load
+// <= 1/3) and rows take a few MB of L2 each while a handful of partitions are in flight.
+constexpr uint64_t L2_PARTITION_ROWS = 1ull << 17;
+
 template <int KW, int PB, int HS>
-Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt) {
+Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt, int force_tables = -1) {
     Plan pl;
     const size_t budget = probe_smem_budget(info);
     // largest table (then largest probe sub-chunk) whose probe block fits two per SM
@@ -125,6 +139,33 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     }
     for (int p = 0; p < 2; p++) {
         if (pl.bits[p] > MAX_RADIX_BITS) pl.bits[p] = MAX_RADIX_BITS;
+    }
+    // Shared-memory tables unless the caller asks for L2 ones: on the 2^27 x 2^29 int64 join
+    // two passes + shared-memory tables take 23.4 ms, one pass + L2 tables 29 ms (builds by
+    // global CAS and lock-step cluster walks are latency-bound).
+    int tables = VJ_TABLES_SHARED;
+    if (opt && (opt->flags & VJ_JOIN_SHARED_TABLES)) tables = VJ_TABLES_SHARED;
+    if (opt && (opt->flags & VJ_JOIN_L2_TABLES)) tables = VJ_TABLES_L2;
+    if (force_tables >= 0) tables = force_tables;
+    if (tables == VJ_TABLES_L2 && nr > 0) {
+        pl.tables = VJ_TABLES_L2;
+        pl.passes = 1;
+        int b = ceil_log2((nr + L2_PARTITION_ROWS - 1) / L2_PARTITION_ROWS);
+        if (opt && (opt->flags & VJ_JOIN_FIXED_PASSES) && opt->radix_bits[0] > 0) b = opt->radix_bits[0];
+        pl.bits[0] = b < 1 ? 1 : (b > MAX_RADIX_BITS ? MAX_RADIX_BITS : b);
+        pl.bits[1] = 0;
+        // a seq holds at most twice the average partition (rounded to a power of two)
+        uint64_t avg = (nr + (1ull << pl.bits[0]) - 1) >> pl.bits[0];
+        uint32_t rc = 4096;
+        while (rc < 2 * avg && rc < (1u << 24)) rc <<= 1;
+        if (opt && opt->build_rows > 0) {  // smaller build chunks: several seqs per partition
+            uint32_t want = 64;
+            while (want < (uint32_t)opt->build_rows && want < rc) want <<= 1;
+            rc = want;
+        }
+        pl.l2_rc = rc;
+        pl.l2_region_slots = l2_cap(rc);
+        if (opt && opt->probe_rows > 0) pl.l2_probe_rows = opt->probe_rows < 32 ? 32u : (uint32_t)opt->probe_rows;
     }
     const int G0 = 2;
     const int G1 = 2 << pl.bits[0];
@@ -225,7 +266,24 @@ struct JoinRun {
     int threads;       // probe block size
     size_t probe_smem;
     int probe_grid;
+    // L2-table build/probe (tables == VJ_TABLES_L2)
+    bool l2 = false;
+    L2Params l2p;
+    size_t l2_smem = 0;
+    int l2_grid = 0;
 };
+
+template <int KW, int PB, int HS>
+int l2_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
+    run->l2 = true;
+    run->l2_smem = (size_t)L2_WARPS * L2_WARP_STAGE * 2 * PB;
+    VJ_TRY(ensure_smem(l2_join_kernel<KW, PB, HS>, run->l2_smem));
+    int per_sm = 0;
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, l2_join_kernel<KW, PB, HS>, L2_THREADS, run->l2_smem));
+    VJ_CHECK(per_sm >= 1, VJ_ERR_UNSUPPORTED, "L2-table probe kernel does not fit an SM");
+    run->l2_grid = per_sm * ctx->info.sms;  // all resident: the cooperative launch checks it
+    return VJ_OK;
+}
 
 template <int KW, int PB, int HS, bool AOS>
 int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
@@ -247,8 +305,23 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     const int np = pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1);
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
-    const uint64_t item_cap = (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    const uint64_t item_cap = pl.tables == VJ_TABLES_L2 ? 0 : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    const bool l2 = pl.tables == VJ_TABLES_L2;
+    const uint32_t max_seqs = l2 ? (uint32_t)(np + in.rows[0] / pl.l2_rc + 1) : 0;
+    // work items when every partition is one seq (more are found by searching group offsets)
+    const uint64_t l2_items_est = l2 ? (uint64_t)in.rows[0] / pl.l2_build_rows + (uint64_t)in.rows[1] / pl.l2_probe_rows + 2ull * max_seqs + 4096 : 0;
+    const uint32_t l2_item_cap = (uint32_t)(l2_items_est < 0xffffffffull ? l2_items_est : 0xffffffffull);
+    L2Params Lq{};
     auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint4 **item_desc, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
+        if (l2) {
+            Lq.tables = c.take<unsigned long long>((size_t)pl.l2_ring * pl.l2_region_slots);
+            Lq.seq = c.take<uint4>(max_seqs);
+            Lq.group_start = c.take<uint32_t>((size_t)max_seqs + pl.l2_lag + 1);
+            Lq.built = c.take<uint32_t>(max_seqs);
+            Lq.probed = c.take<uint32_t>(max_seqs);
+            Lq.nseq = c.take<uint32_t>(4);
+            Lq.items = c.take<uint4>(l2_item_cap);
+        }
         for (int pass = 0; pass < 2; pass++) {
             for (int sd = 0; sd < 2; sd++) {
                 bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
@@ -349,6 +422,31 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     run->probe = Pq;
     run->d_out_count = out_count;
     run->d_error = error;
+    if (l2) {
+        Lq.r_rows = bufs[0][0];
+        Lq.s_rows = bufs[0][1];
+        Lq.r_begin = seg_begin;
+        Lq.r_end = seg_end;
+        Lq.s_begin = seg_begin + np;
+        Lq.s_end = seg_end + np;
+        Lq.np = np;
+        Lq.part_bits = pl.bits[0];
+        Lq.rc = pl.l2_rc;
+        Lq.build_rows = pl.l2_build_rows;
+        Lq.probe_rows = pl.l2_probe_rows;
+        Lq.ring = pl.l2_ring;
+        Lq.lag = pl.l2_lag;
+        Lq.region_slots = pl.l2_region_slots;
+        Lq.max_seqs = max_seqs;
+        Lq.item_cap = l2_item_cap;
+        Lq.ticket = ticket;
+        Lq.out_count = out_count;
+        Lq.outcap = pl.l2_outcap;
+        Lq.hs = hs;
+        Lq.error = error;
+        run->l2p = Lq;
+        return l2_setup<KW, PB, HS>(ctx, pl, run);
+    }
     if (pl.passes == 0) {
         return probe_setup<KW, PB, HS, false>(ctx, pl, run);
     }
@@ -358,6 +456,21 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
 template <int KW, int PB, int HS>
 int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
     profile_mark(ctx, PM_PROBE_BEGIN, stream);
+    if (run.l2) {
+        L2Params q = run.l2p;
+        q.out = run.probe.out;
+        q.capacity = run.probe.capacity;
+        // slots left by an earlier probe carry the tags this one reuses
+        VJ_CUDA(cudaMemsetAsync(q.tables, 0, (size_t)q.ring * q.region_slots * sizeof(unsigned long long), stream));
+        l2_plan_kernel<<<1, PLAN_THREADS, 0, stream>>>(q);
+        VJ_CUDA(cudaGetLastError());
+        // its blocks wait for one another's items: all must be resident
+        void *args[] = {&q};
+        VJ_CUDA(cudaLaunchCooperativeKernel((const void *)l2_join_kernel<KW, PB, HS>, dim3(run.l2_grid), dim3(L2_THREADS), args, run.l2_smem, stream));
+        profile_mark(ctx, PM_PROBE_END, stream);
+        ctx->launches += 2;
+        return VJ_OK;
+    }
     plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
     VJ_CUDA(cudaGetLastError());
     if (run.aos) {
@@ -379,8 +492,10 @@ void finish_profile(vj_ctx *ctx, const Plan &pl, uint64_t nr, uint64_t ns, uint6
     p.kernel_launches = ctx->launches;
     p.radix_bits[0] = pl.bits[0];
     p.radix_bits[1] = pl.bits[1];
-    p.build_rows = pl.rcap;
-    p.probe_rows = pl.schunk;
+    p.build_rows = pl.tables == VJ_TABLES_L2 ? pl.l2_rc : pl.rcap;
+    p.probe_rows = pl.tables == VJ_TABLES_L2 ? pl.l2_probe_rows : pl.schunk;
+    p.tables = pl.tables;
+    p.fallbacks = pl.fallbacks;
     p.rows[0] = nr;
     p.rows[1] = ns;
     p.matches = matches;
@@ -402,7 +517,8 @@ void finish_profile(vj_ctx *ctx, const Plan &pl, uint64_t nr, uint64_t ns, uint6
     p.ms_total = ms(pl.passes ? PM_PASS0 : PM_PROBE_BEGIN, PM_PROBE_END);
 }
 
-int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count) {
+// Match count and the kernels' error flags of the probe just launched (synchronises).
+int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count, uint32_t *flags) {
     static thread_local unsigned long long *pinned = nullptr;
     if (!pinned) {
         VJ_CUDA(cudaMallocHost(&pinned, 2 * sizeof(unsigned long long)));
@@ -411,8 +527,38 @@ int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count) {
     VJ_CUDA(cudaMemcpyAsync(&pinned[0], run.d_out_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
     VJ_CUDA(cudaMemcpyAsync(&pinned[1], run.d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
     VJ_CUDA(cudaStreamSynchronize(stream));
-    VJ_CHECK((pinned[1] & 0xffffffffull) == 0, VJ_ERR_DEVICE, "probe kernel reported an internal limit (flags %llx)", pinned[1]);
+    *flags = (uint32_t)pinned[1];
     *count = pinned[0];
+    return VJ_OK;
+}
+
+int check_flags(uint32_t flags) {
+    VJ_CHECK(flags == 0, VJ_ERR_DEVICE, "probe kernel reported an internal limit (flags %x)", flags);
+    return VJ_OK;
+}
+
+// Plan, partition and probe once into (out, capacity); a plan with L2 tables that meets a
+// long duplicate cluster (error flag 8) is redone with shared-memory tables, whose
+// per-chunk tables bound the cost of duplicates. On return `run` holds the partitions of
+// the plan that succeeded (for a second probe into a larger buffer).
+template <int KW, int PB, int HS>
+int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, int force_tables, void *out, uint64_t capacity, cudaStream_t stream, JoinRun *run, Plan *plan,
+               uint64_t *count) {
+    Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt, force_tables);
+    *run = JoinRun{};
+    VJ_TRY((prepare<KW, PB, HS>(ctx, t, pl, hs, stream, run)));
+    run->probe.out = out;
+    run->probe.capacity = capacity;
+    VJ_TRY((launch_probe<KW, PB, HS>(ctx, *run, stream)));
+    uint32_t flags = 0;
+    VJ_TRY(read_count(*run, stream, count, &flags));
+    if ((flags & 8u) && pl.tables == VJ_TABLES_L2) {
+        VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, VJ_TABLES_SHARED, out, capacity, stream, run, plan, count)));
+        plan->fallbacks += 1;
+        return VJ_OK;
+    }
+    VJ_TRY(check_flags(flags));
+    *plan = pl;
     return VJ_OK;
 }
 
@@ -420,9 +566,6 @@ int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count) {
 
 template <int KW, int PB, int HS>
 int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, vj_result *res, cudaStream_t stream) {
-    const Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt);
-    JoinRun run;
-    VJ_TRY((prepare<KW, PB, HS>(ctx, t, pl, hs, stream, &run)));
     const bool caller_buffer = res->pairs != nullptr && res->capacity > 0 && !res->owned;
     if (!caller_buffer) {
         uint64_t cap = t.rows[1] ? t.rows[1] : 1;
@@ -433,11 +576,10 @@ int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
         res->owned = 1;
     }
     res->payload_bytes = PB;
-    run.probe.out = res->pairs;
-    run.probe.capacity = res->capacity;
-    VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
+    Plan pl;
+    JoinRun run;
     uint64_t count = 0;
-    VJ_TRY(read_count(run, stream, &count));
+    VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, -1, res->pairs, res->capacity, stream, &run, &pl, &count)));
     finish_profile(ctx, pl, t.rows[0], t.rows[1], count);
     if (count > res->capacity) {
         if (!res->owned) {
@@ -458,7 +600,9 @@ int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
         run.probe.capacity = count;
         VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
         uint64_t again = 0;
-        VJ_TRY(read_count(run, stream, &again));
+        uint32_t flags = 0;
+        VJ_TRY(read_count(run, stream, &again, &flags));
+        VJ_TRY(check_flags(flags));
         VJ_CHECK(again == count, VJ_ERR_DEVICE, "second probe gave %llu pairs, first %llu", (unsigned long long)again, (unsigned long long)count);
     }
     res->count = count;
@@ -627,14 +771,10 @@ struct BuildProbeCall {
     template <int KW, int PB, int HS>
     int run() {
         vj_result &rr = *c.res;
-        Plan pl = make_plan<KW, PB, HS>(c.t.rows[0], c.t.rows[1], c.ctx->info, nullptr);
+        Plan pl;
         JoinRun run;
-        VJ_TRY((prepare<KW, PB, HS>(c.ctx, c.t, pl, c.hs, c.stream, &run)));
-        run.probe.out = rr.pairs;
-        run.probe.capacity = rr.capacity;
-        VJ_TRY((launch_probe<KW, PB, HS>(c.ctx, run, c.stream)));
         uint64_t n = 0;
-        VJ_TRY(read_count(run, c.stream, &n));
+        VJ_TRY((probe_once<KW, PB, HS>(c.ctx, c.t, c.hs, nullptr, -1, rr.pairs, rr.capacity, c.stream, &run, &pl, &n)));
         finish_profile(c.ctx, pl, c.t.rows[0], c.t.rows[1], n);
         rr.count = n;
         return VJ_OK;

@@ -735,8 +735,8 @@ __device__ __forceinline__ uint4 item_rows(const ProbeParams &Q, uint32_t it, bo
 // End of a probe sub-chunk (all threads): reserve the output range of the buffer just
 // filled (one atomic, whose result is read one sub-chunk later), copy out the buffer
 // filled before it, and switch buffers. The atomic's latency overlaps a sub-chunk of work.
-template <int PB>
-__device__ __forceinline__ void rotate_stage(const ProbeParams &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
+template <int PB, typename QP>
+__device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
                                              unsigned long long *pend_base) {
     using PT = typename Pair<PB>::T;
     __syncthreads();

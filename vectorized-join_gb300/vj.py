@@ -21,6 +21,8 @@ VJ_ERR_CAPACITY = 5
 VJ_ERR_DEVICE = 6
 VJ_ERR_BUDGET = 7
 VJ_JOIN_FIXED_PASSES = 1
+VJ_JOIN_SHARED_TABLES = 2
+VJ_JOIN_L2_TABLES = 4
 
 ALGORITHMS = [
     "fnv",
@@ -113,6 +115,8 @@ class VjProfile(ctypes.Structure):
         ("ms_total", ctypes.c_float),
         ("rows", ctypes.c_uint64 * 2),
         ("matches", ctypes.c_uint64),
+        ("tables", ctypes.c_int32),
+        ("fallbacks", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -129,6 +133,8 @@ class VjProfile(ctypes.Structure):
             "ms_total": self.ms_total,
             "rows": list(self.rows),
             "matches": self.matches,
+            "tables": "l2" if self.tables == 1 else "shared",
+            "fallbacks": self.fallbacks,
         }
 
 
@@ -259,12 +265,14 @@ def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTa
     return t
 
 
-def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, probe_sub_rows: int = 0) -> VjJoinOptions:
+def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, probe_sub_rows: int = 0, tables: str = "auto") -> VjJoinOptions:
+    """Join options; tables: "auto", "shared" (shared-memory tables) or "l2" (L2-resident tables)."""
     o = VjJoinOptions()
     o.hash_algo = hash_algo
     o.hash_bits = hash_bits
+    o.flags = {"auto": 0, "shared": VJ_JOIN_SHARED_TABLES, "l2": VJ_JOIN_L2_TABLES}[tables]
     if passes is not None:
-        o.flags = VJ_JOIN_FIXED_PASSES
+        o.flags |= VJ_JOIN_FIXED_PASSES
         o.passes = passes
     o.radix_bits[0] = radix_bits[0]
     o.radix_bits[1] = radix_bits[1]
