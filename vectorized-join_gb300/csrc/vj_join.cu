@@ -59,11 +59,13 @@ int ceil_log2(uint64_t x) {
     return b;
 }
 
-// Shared memory a probe block may use: two resident blocks per SM.
-size_t probe_smem_budget(const DeviceInfo &info) {
-    size_t per_block = info.smem_optin ? info.smem_optin : 48 * 1024;
-    size_t two = (228 * 1024) / 2 - 2048;  // 2 blocks per SM, minus per-block reservations
-    return per_block < two ? per_block : two;
+// Shared memory a probe block may use: blocks of `threads` resident 1024 threads per SM
+// (two blocks of 512, four of 256, ...).
+size_t probe_smem_budget(const DeviceInfo &info, int threads) {
+    const size_t per_block = info.smem_optin ? info.smem_optin : 48 * 1024;
+    const int blocks = threads >= 512 ? 2 : 1024 / threads;
+    const size_t share = (228 * 1024) / blocks - 2048;  // minus per-block reservations
+    return per_block < share ? per_block : share;
 }
 
 // Build rows per partition the L2-table plan aims at: its table (8-byte slots, load
@@ -73,7 +75,11 @@ constexpr uint64_t L2_PARTITION_ROWS = 1ull << 17;
 template <int KW, int PB, int HS>
 Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt, int force_tables = -1) {
     Plan pl;
-    const size_t budget = probe_smem_budget(info);
+    if (opt && opt->probe_threads > 0) {
+        int t = opt->probe_threads / 32 * 32;
+        pl.threads = t < 64 ? 64 : (t > PROBE_THREADS ? PROBE_THREADS : t);
+    }
+    const size_t budget = probe_smem_budget(info, pl.threads);
     // largest table (then largest probe sub-chunk) whose probe block fits two per SM
     bool found = false;
     for (uint32_t sub = 1024; sub >= 256 && !found; sub >>= 1) {
@@ -88,10 +94,6 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
                 break;
             }
         }
-    }
-    if (opt && opt->probe_threads > 0) {
-        int t = opt->probe_threads / 32 * 32;
-        pl.threads = t < 64 ? 64 : (t > PROBE_THREADS ? PROBE_THREADS : t);
     }
     if (opt && opt->probe_sub_rows > 0) {
         uint32_t sub = (uint32_t)opt->probe_sub_rows;
