@@ -272,6 +272,212 @@ def run_e2e(args, ctx, vj, torch, stream, dev, world, rk, rp, sk, sp, nr, ns, m,
     }
 
 
+# ---------------------------------------------------------------- other workloads
+#
+# `--workload` selects one of the other measured shapes; each prints one JSON line with the
+# same base keys. The default (the 2^27 x 2^29 int64 join) is the headline.
+
+
+def _timed(torch, stream, fn, steps: int, warmup: int):
+    """Per-step device times (ms) of fn() with CUDA events on `stream`, after warm-up."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for i in range(steps):
+        fn()
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    return [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+
+
+def _latency(ms: list) -> dict:
+    q = sorted(ms)
+    return {"p50": q[len(q) // 2], "p99": q[min(len(q) - 1, int(round(0.99 * (len(q) - 1))))], "min": q[0], "max": q[-1]}
+
+
+def _base_line(metric, value, unit, steps, warmup, ms, dtype, cfg, hib=True):
+    return {
+        "metric": metric,
+        "value": value,
+        "unit": unit,
+        "n_gpus": 1,
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": ms,
+        "higher_is_better": hib,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": dtype,
+        "data": "synthetic (seeded, generated on the device)",
+        "config": cfg,
+    }
+
+
+def run_small_join(args) -> None:
+    """int32 keys and payloads, R = 2^20 unique keys, S = 2^22 drawn from R (100% match),
+    FNV-1a 32, one radix pass of 8 bits. The working set (~42 MB) fits in L2."""
+    import torch
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+    oracle = _import(ROOT / "oracle" / "oracle.py", "vj_oracle")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nr, ns = 1 << 20, 1 << 22
+    thr = 1 << 32
+    rk = torch.empty(nr, dtype=torch.int32, device=dev)
+    rp = torch.empty_like(rk)
+    sk = torch.empty(ns, dtype=torch.int32, device=dev)
+    sp = torch.empty_like(sk)
+    vj.generate_join(SEED, 4, 4, nr, ns, thr, rk, rp, sk, sp)
+    expect = vj.generate_join_expect(SEED, nr, ns, thr)
+    out = torch.empty((expect[0], 2), dtype=torch.int32, device=dev)
+    ctx = vj.Context(0)
+    ctx.set_profiling(True)
+    t_r, t_s = vj.table(rk, rp, nr, 1, 4), vj.table(sk, sp, ns, 1, 4)
+    opts = vj.options(hash_bits=32, passes=1, radix_bits=(8, 0))
+    stream = torch.cuda.current_stream()
+    res = ctx.join(t_r, t_s, opts, out=out, capacity=expect[0], stream=stream)
+    assert res.count == expect[0] and vj.pairs_digest(out, res.count, 4) == (expect[1], expect[2])
+    steps = max(args.steps, 30)
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = _timed(torch, stream, lambda: ctx.join(t_r, t_s, opts, out=out, capacity=expect[0], stream=stream), steps, args.warmup)
+    clocks = sampler.stop()
+    t = sum(ms) / len(ms)
+    n = nr + ns
+    b_alg = n * (1 * (4 + 2 * 8) + 8) + expect[0] * 2 * 4
+    peak, src = measured_peak()
+    cfg = {"workload": "int32 FK join 2^20 x 2^22, 100% match, FNV-1a 32, 1 radix pass of 8 bits", "r_rows": nr, "s_rows": ns, "l2_policy": "working set ~42 MB fits in L2: L2, not HBM, bounds it"}
+    line = _base_line(METRIC, n / (t / 1000), UNIT, steps, args.warmup, t, "int32", cfg)
+    line["join_roofline"] = {"bytes_alg_per_join": b_alg, "achieved": b_alg / (t / 1000) / 1e9, "peak": peak, "unit": "GB/s", "frac": b_alg / (t / 1000) / 1e9 / peak, "peak_source": src}
+    line["latency_ms"] = _latency(ms)
+    line["stages_ms"] = ctx.last_profile().as_dict()
+    line["clocks"] = clocks
+    # the oracle on the host cores, same inputs
+    g = oracle.gen_join(SEED, 4, nr, ns, 1.0)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    runs = 0
+    while time.perf_counter() - t0 < 5.0:
+        cnt, _, _ = oracle.join(g["r_keys"], g["r_pay"], g["s_keys"], g["s_pay"], hash_bits=32, radix_bits=8, threads=threads, want_pairs=False)
+        runs += 1
+    assert cnt == expect[0]
+    dt = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": n * runs / dt, "unit": UNIT, "cores": threads, "kind": "port", "sample": f"the full workload, {runs} joins in {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
+def run_skew_join(args) -> None:
+    """R = 2^26 unique int64 keys, S = 2^28 keys drawn Zipf(s = 1.0) over R's keys: the heavy
+    hitters crowd a few partitions and probe chains."""
+    import torch
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    nr, ns = 1 << 26, 1 << 28
+    rk = torch.empty(nr, dtype=torch.int64, device=dev)
+    rp = torch.empty_like(rk)
+    dummy_k = torch.empty(1, dtype=torch.int64, device=dev)
+    dummy_p = torch.empty(1, dtype=torch.int64, device=dev)
+    vj.generate_join(SEED, 8, 8, nr, 1, 0, rk, rp, dummy_k, dummy_p)  # unique R keys, payload = row id
+    # Zipf(1.0) ranks by inverse CDF (double precision); rank r -> a random build row
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    w = 1.0 / torch.arange(1, nr + 1, dtype=torch.float64, device=dev)
+    cdf = torch.cumsum(w, 0)
+    cdf /= cdf[-1].clone()
+    del w
+    perm = torch.randperm(nr, generator=gen, device=dev)
+    ridx = torch.empty(ns, dtype=torch.int64, device=dev)
+    chunk = 1 << 25
+    for a in range(0, ns, chunk):
+        u = torch.rand(chunk, dtype=torch.float64, generator=gen, device=dev)
+        ridx[a : a + chunk] = perm[torch.clamp(torch.searchsorted(cdf, u), max=nr - 1)]
+    del cdf, perm
+    sk = rk[ridx]
+    sp = torch.arange(ns, dtype=torch.int64, device=dev)
+    want = torch.stack([rp[ridx], sp], dim=1).contiguous()
+    want_digest = vj.pairs_digest(want, ns, 8)
+    del want, ridx
+    out = torch.empty((ns, 2), dtype=torch.int64, device=dev)
+    ctx = vj.Context(0)
+    ctx.set_profiling(True)
+    t_r, t_s = vj.table(rk, rp, nr, 2, 8), vj.table(sk, sp, ns, 2, 8)
+    stream = torch.cuda.current_stream()
+    res = ctx.join(t_r, t_s, None, out=out, capacity=ns, stream=stream)
+    assert res.count == ns and vj.pairs_digest(out, res.count, 8) == want_digest
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = _timed(torch, stream, lambda: ctx.join(t_r, t_s, None, out=out, capacity=ns, stream=stream), args.steps, args.warmup)
+    clocks = sampler.stop()
+    prof = ctx.last_profile().as_dict()
+    t = sum(ms) / len(ms)
+    n = nr + ns
+    b_alg = n * (2 * (8 + 2 * 16) + 16) + ns * 2 * 8
+    peak, src = measured_peak()
+    cfg = {"workload": "int64 skew join 2^26 unique x 2^28 Zipf(1.0) over R, 100% match, FNV-1a 64, 2 radix passes", "r_rows": nr, "s_rows": ns, "l2_policy": "inputs (5 GiB) larger than L2"}
+    line = _base_line(METRIC, n / (t / 1000), UNIT, args.steps, args.warmup, t, "int64", cfg)
+    line["join_roofline"] = {"bytes_alg_per_join": b_alg, "achieved": b_alg / (t / 1000) / 1e9, "peak": peak, "unit": "GB/s", "frac": b_alg / (t / 1000) / 1e9 / peak, "peak_source": src}
+    line["latency_ms"] = _latency(ms)
+    line["stages_ms"] = prof
+    line["clocks"] = clocks
+    print(json.dumps(line), flush=True)
+
+
+def run_hash_bench(args) -> None:
+    """hash_func over 2^30 keys of 8, 16 and 32 uniform random bytes, FNV-1a 64 and the
+    custom hash (custom_xor_hw), 64-bit chunks. Bytes = n * (key bytes + 8)."""
+    import numpy as np
+    import torch
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+    oracle = _import(ROOT / "oracle" / "oracle.py", "vj_oracle")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = 1 << 30
+    peak, src = measured_peak()
+    stream = torch.cuda.current_stream()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    results = []
+    sampler = ClockSampler(0)
+    sampler.start()
+    for eb in (8, 16, 32):
+        keys = torch.randint(-(2**62), 2**62, (n * eb // 8,), dtype=torch.int64, generator=gen, device=dev)
+        hashes = torch.empty(n, dtype=torch.int64, device=dev)
+        for algo in ("fnv", "custom_xor_hw"):
+            call = lambda: vj.hash(keys, n, 0, eb // 8, 64, 64, algo, hashes, stream=stream)
+            call()
+            torch.cuda.synchronize()
+            k = 4096
+            words = keys[: k * eb // 8].cpu().numpy().view(np.uint32).reshape(k, eb // 4)
+            want, _ = oracle.hash_elements(words, k, 0, eb // 8, 64, 64, algo)
+            assert np.array_equal(hashes[:k].cpu().numpy().view(np.uint64), want.astype(np.uint64)), (eb, algo)
+            ms = _timed(torch, stream, call, args.steps, args.warmup)
+            t = sum(ms) / len(ms)
+            gbs = n * (eb + 8) / (t / 1000) / 1e9
+            results.append({"key_bytes": eb, "algo": algo, "ms": t, "GB/s": gbs, "frac": gbs / peak, "keys_per_s": n / (t / 1000)})
+        del keys, hashes
+        torch.cuda.empty_cache()
+    clocks = sampler.stop()
+    head = next(r for r in results if r["key_bytes"] == 16 and r["algo"] == "fnv")
+    cfg = {"workload": "hash 2^30 keys x {8,16,32} B, FNV-1a 64 and custom_xor_hw, 64-bit chunks", "keys": n, "l2_policy": "inputs 8-32 GiB, larger than L2"}
+    line = _base_line("hash throughput (bytes read + written / s) on 1 GB300", head["GB/s"], "GB/s", args.steps, args.warmup, head["ms"], "u64", cfg)
+    line["roofline"] = {"kernel": "hash_kernel", "bound": "hbm", "achieved": head["GB/s"], "peak": peak, "unit": "GB/s", "frac": head["frac"], "traffic": None, "peak_source": src}
+    line["cases"] = results
+    line["clocks"] = clocks
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -283,8 +489,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.impl == "ours" and args.workload != "join":
+        {"join-small": run_small_join, "join-skew": run_skew_join, "hash": run_hash_bench}[args.workload](args)
+        return
     if args.small:
         args.shift = max(args.shift, 3)
     args.small = args.shift > 0
