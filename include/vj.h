@@ -258,6 +258,26 @@ VJ_API int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const
 
 VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
 
+/*
+ * vj_join_batch -- many independent joins in one launch sequence. The reference runs one
+ * JoinProvider::join per call; its nearest counterpart is the bucket-pair work list of a
+ * single join (src/join/join_provider.cuh:717-795).
+ * Join j joins build rows [d_r_offsets[j], d_r_offsets[j+1]) of r with probe rows
+ * [d_s_offsets[j], d_s_offsets[j+1]) of s (device arrays of joins + 1 uint64_t, starting
+ * at 0, ending at the table's rows, non-decreasing). Its pairs (r payload, s payload) go to
+ * d_pairs[d_pair_offsets[j] .. d_pair_offsets[j+1]) (pair_capacity pairs in all) and their
+ * number to d_counts[j]; a count above the join's range means the pairs past the range
+ * were dropped. max_build_rows: the largest join's build rows (plans the radix pass; 0 =
+ * all of r). *d_status (device, optional) receives the kernels' flags: 0 = ok, 16 = an
+ * offset was out of range or decreasing and was clamped (that join's results are then
+ * unspecified). Asynchronous: no host synchronisation, and once the context's workspace
+ * has grown to a batch of this shape, no allocation -- repeated calls can be captured in
+ * a CUDA graph after one call outside the capture. Each join's pairs equal vj_join's on
+ * the same rows.
+ */
+VJ_API int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, uint32_t joins, const uint64_t *d_r_offsets, const uint64_t *d_s_offsets, uint64_t max_build_rows,
+                         const vj_join_options *options, void *d_pairs, const uint64_t *d_pair_offsets, uint64_t pair_capacity, uint64_t *d_counts, uint32_t *d_status, vj_stream_t stream);
+
 /* Order-independent digest of a pair list: sum and xor of a 64-bit mix of each pair, the
  * same function the CPU oracle computes. For comparing full-size joins without sorting.
  * Synchronises stream. */

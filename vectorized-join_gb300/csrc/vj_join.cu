@@ -256,7 +256,54 @@ int probe_grid(const DeviceInfo &info, int threads, size_t smem, int *grid) {
 struct Tables {
     const void *keys[2], *pay[2], *hash[2];
     uint32_t rows[2];
+    // a batch of independent joins (r_offsets set): join j is build rows
+    // [r_offsets[j], r_offsets[j+1]) and probe rows [s_offsets[j], s_offsets[j+1]); its
+    // pairs go to pair_offsets[j] .. pair_offsets[j+1] of the output, counted in counts[j]
+    uint32_t joins = 1;
+    const unsigned long long *r_offsets = nullptr, *s_offsets = nullptr, *pair_offsets = nullptr;
+    unsigned long long pair_capacity = 0;
+    unsigned long long *counts = nullptr;
 };
+
+// Segments of a batch from the caller's offsets, each range clamped into its table (and
+// the output ranges into the output buffer) so that no later kernel can leave its buffers;
+// error flag 16 when an offset had to be clamped.
+__global__ void batch_segments_kernel(uint32_t joins, const unsigned long long *ro, const unsigned long long *so, const unsigned long long *po, uint32_t r_rows, uint32_t s_rows,
+                                      unsigned long long pair_cap, uint32_t *seg_begin, uint32_t *seg_end, unsigned long long *out_begin, uint32_t *error) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j <= joins; j += gridDim.x * blockDim.x) {
+        bool bad = false;
+        auto clamp = [&](unsigned long long v, unsigned long long lo, unsigned long long hi) -> unsigned long long {
+            const unsigned long long c = v < lo ? lo : (v > hi ? hi : v);
+            bad |= c != v;
+            return c;
+        };
+        // ranges start at 0, end at the table's rows and never decrease
+        out_begin[j] = clamp(po[j], 0, pair_cap);
+        if (j < joins) {
+            const unsigned long long rb = j == 0 ? clamp(ro[0], 0, 0) : clamp(ro[j], 0, r_rows);
+            const unsigned long long sb = j == 0 ? clamp(so[0], 0, 0) : clamp(so[j], 0, s_rows);
+            const unsigned long long re = j + 1 == joins ? clamp(ro[j + 1], r_rows, r_rows) : clamp(ro[j + 1], rb, r_rows);
+            const unsigned long long se = j + 1 == joins ? clamp(so[j + 1], s_rows, s_rows) : clamp(so[j + 1], sb, s_rows);
+            bad |= po[j + 1] < po[j];
+            seg_begin[j] = (uint32_t)rb;
+            seg_end[j] = (uint32_t)(re < rb ? rb : re);
+            seg_begin[joins + j] = (uint32_t)sb;
+            seg_end[joins + j] = (uint32_t)(se < sb ? sb : se);
+        }
+        if (bad) atomicOr(error, 16u);
+    }
+}
+
+// Output ranges must not decrease: a running maximum over the (clamped) pair offsets.
+__global__ void batch_out_monotone_kernel(uint32_t joins, unsigned long long *out_begin) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long m = 0;
+        for (uint32_t j = 0; j <= joins; j++) {
+            if (out_begin[j] < m) out_begin[j] = m;
+            m = out_begin[j];
+        }
+    }
+}
 
 struct JoinRun {
     // results
@@ -268,6 +315,9 @@ struct JoinRun {
     int threads;       // probe block size
     size_t probe_smem;
     int probe_grid;
+    // batches of joins: per-join item counts, partitions per join
+    uint32_t *batch_cnt = nullptr;
+    uint32_t batch_parts = 1;
     // L2-table build/probe (tables == VJ_TABLES_L2)
     bool l2 = false;
     L2Params l2p;
@@ -303,11 +353,22 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     using L = Layout<KW, PB, HS>;
     const int bins0 = 1 << pl.bits[0];
     const int bins1 = 1 << pl.bits[1];
-    const int G0 = 2, G1 = 2 * bins0;
-    const int np = pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1);
+    const bool batch = in.r_offsets != nullptr;
+    const int J = batch ? (int)in.joins : 1;  // segments per side entering the first pass
+    const int G0 = 2 * J, G1 = 2 * J * bins0;
+    const int np = J * (pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1));
+    int max_units[2] = {pl.max_units[0], pl.max_units[1]};
+    if (batch) {
+        max_units[0] = ctx->info.sms * 16 + G0;
+        max_units[1] = ctx->info.sms * 16 + G1;
+    }
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
-    const uint64_t item_cap = pl.tables == VJ_TABLES_L2 ? 0 : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    const uint64_t item_cap = pl.tables == VJ_TABLES_L2 ? 0
+                              : batch                     ? 2ull * ((uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap) + 4096
+                                                          : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    uint32_t *b_seg_begin = nullptr, *b_seg_end = nullptr, *b_cnt = nullptr;
+    unsigned long long *b_out_begin = nullptr;
     const bool l2 = pl.tables == VJ_TABLES_L2;
     const uint32_t max_seqs = l2 ? (uint32_t)(np + in.rows[0] / pl.l2_rc + 1) : 0;
     // work items when every partition is one seq (more are found by searching group offsets)
@@ -329,8 +390,14 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
                 bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
             }
         }
-        if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, pl.max_units[0]);
-        if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, pl.max_units[1]);
+        if (batch) {
+            b_seg_begin = c.take<uint32_t>((size_t)2 * J);
+            b_seg_end = c.take<uint32_t>((size_t)2 * J);
+            b_cnt = c.take<uint32_t>((size_t)J);
+            b_out_begin = c.take<unsigned long long>((size_t)J + 1);
+        }
+        if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, max_units[0]);
+        if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, max_units[1]);
         *item_begin = c.take<uint32_t>((size_t)np + 2);
         *item_desc = c.take<uint4>(item_cap);
         *ticket = c.take<uint32_t>(1);
@@ -354,6 +421,17 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
 
     const uint32_t *seg_begin = nullptr, *seg_end = nullptr;
     int Q = 1;
+    if (batch) {
+        batch_segments_kernel<<<(J + 256) / 256, 256, 0, stream>>>(in.joins, in.r_offsets, in.s_offsets, in.pair_offsets, in.rows[0], in.rows[1], in.pair_capacity, b_seg_begin, b_seg_end, b_out_begin,
+                                                                     error);
+        VJ_CUDA(cudaGetLastError());
+        batch_out_monotone_kernel<<<1, 1, 0, stream>>>(in.joins, b_out_begin);
+        VJ_CUDA(cudaGetLastError());
+        ctx->launches += 2;
+        seg_begin = b_seg_begin;
+        seg_end = b_seg_end;
+        Q = J;
+    }
     int consumed_bits = 0;
     for (int pass = 0; pass < pl.passes; pass++) {
         PassParams P{};
@@ -373,7 +451,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         consumed_bits += pl.bits[pass];
         P.shift = 64 - consumed_bits;  // top bits of the mixed hash, pass 1 first
         P.hs = hs;
-        P.max_units = pl.max_units[pass];
+        P.max_units = max_units[pass];
         P.min_unit_rows = 4096;
         P.error = error;
         const PassBufs &pb = pass == 0 ? pb0 : pb1;
@@ -396,7 +474,10 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.s_hash = in.hash[1];
     if (pl.passes == 0) {
         Pq.r_rows_in = Pq.s_rows_in = nullptr;
-        Pq.r_begin = Pq.r_end = Pq.s_begin = Pq.s_end = nullptr;
+        Pq.r_begin = seg_begin;  // a batch: one partition per join; else the whole tables
+        Pq.r_end = seg_end;
+        Pq.s_begin = seg_begin ? seg_begin + np : nullptr;
+        Pq.s_end = seg_end ? seg_end + np : nullptr;
     } else {
         Pq.r_rows_in = bufs[pl.passes - 1][0];
         Pq.s_rows_in = bufs[pl.passes - 1][1];
@@ -421,6 +502,14 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.out_count = out_count;
     Pq.hs = hs;
     Pq.error = error;
+    Pq.joins = (uint32_t)J;
+    if (batch) {
+        Pq.s_join_begin = b_seg_begin + J;
+        Pq.out_begin = b_out_begin;
+        Pq.out_counts = in.counts;
+        run->batch_cnt = b_cnt;
+        run->batch_parts = (uint32_t)(np / J);
+    }
     run->probe = Pq;
     run->d_out_count = out_count;
     run->d_error = error;
@@ -473,8 +562,19 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         ctx->launches += 2;
         return VJ_OK;
     }
-    plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
-    VJ_CUDA(cudaGetLastError());
+    if (run.probe.out_begin) {
+        const ProbeParams &Q = run.probe;
+        batch_items_kernel<true><<<Q.joins, 256, 0, stream>>>(Q, run.batch_parts, run.batch_cnt, nullptr);
+        VJ_CUDA(cudaGetLastError());
+        batch_scan_kernel<<<1, PLAN_THREADS, 0, stream>>>(Q, run.batch_cnt);
+        VJ_CUDA(cudaGetLastError());
+        batch_items_kernel<false><<<Q.joins, 256, 0, stream>>>(Q, run.batch_parts, nullptr, run.batch_cnt);
+        VJ_CUDA(cudaGetLastError());
+        ctx->launches += 2;
+    } else {
+        plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
+        VJ_CUDA(cudaGetLastError());
+    }
     if (run.aos) {
         probe_kernel<KW, PB, HS, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     } else {
@@ -783,11 +883,91 @@ struct BuildProbeCall {
     }
 };
 
+// A batch of joins: one launch sequence, no host synchronisation. At most one radix pass
+// (the second pass's bookkeeping would grow with joins x buckets x buckets).
+template <int KW, int PB, int HS>
+int batch_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, uint64_t max_build_rows, void *pairs, uint32_t *d_status, cudaStream_t stream) {
+    Plan pl = make_plan<KW, PB, HS>(max_build_rows, 4 * max_build_rows, ctx->info, opt, VJ_TABLES_SHARED);
+    if (pl.passes == 2) {
+        pl.passes = 1;
+        pl.bits[0] = pl.bits[0] + pl.bits[1] > MAX_RADIX_BITS ? MAX_RADIX_BITS : pl.bits[0] + pl.bits[1];
+        pl.bits[1] = 0;
+    }
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;  // stage events need a synchronisation this call does not make
+    JoinRun run;
+    int st = prepare<KW, PB, HS>(ctx, t, pl, hs, stream, &run);
+    if (st == VJ_OK) {
+        run.probe.out = pairs;
+        run.probe.capacity = t.pair_capacity;
+        st = launch_probe<KW, PB, HS>(ctx, run, stream);
+    }
+    ctx->profiling = prof;
+    VJ_TRY(st);
+    if (d_status) VJ_CUDA(cudaMemcpyAsync(d_status, run.d_error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+    return VJ_OK;
+}
+
+struct BatchCall {
+    vj_ctx *ctx;
+    Tables t;
+    HashSpec hs;
+    const vj_join_options *opt;
+    uint64_t max_build_rows;
+    void *pairs;
+    uint32_t *status;
+    cudaStream_t stream;
+    template <int KW, int PB, int HS>
+    int run() {
+        return batch_typed<KW, PB, HS>(ctx, t, hs, opt, max_build_rows, pairs, status, stream);
+    }
+};
+
 }  // namespace
 
 }  // namespace vj
 
 using namespace vj;
+
+extern "C" int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, uint32_t joins, const uint64_t *d_r_offsets, const uint64_t *d_s_offsets, uint64_t max_build_rows,
+                             const vj_join_options *options, void *d_pairs, const uint64_t *d_pair_offsets, uint64_t pair_capacity, uint64_t *d_counts, uint32_t *d_status, vj_stream_t stream) {
+    VJ_CHECK(ctx != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null context");
+    VJ_TRY(check_table(r, "vj_join_batch: r"));
+    VJ_TRY(check_table(s, "vj_join_batch: s"));
+    VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: r and s must have the same key_words and payload_bytes");
+    VJ_CHECK(joins >= 1 && joins <= (1u << 22), VJ_ERR_UNSUPPORTED, "vj_join_batch: joins must be in [1, 2^22] (got %u)", joins);
+    VJ_CHECK(d_r_offsets && d_s_offsets && d_pair_offsets && d_counts, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null offsets or counts");
+    VJ_CHECK(d_pairs != nullptr || pair_capacity == 0, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null output with capacity > 0");
+    VJ_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (r->rows == 0 || s->rows == 0) {  // nothing matches: zero counts, ok status
+        VJ_CUDA(cudaMemsetAsync(d_counts, 0, (size_t)joins * sizeof(uint64_t), st));
+        if (d_status) VJ_CUDA(cudaMemsetAsync(d_status, 0, sizeof(uint32_t), st));
+        return VJ_OK;
+    }
+    BatchCall call;
+    call.ctx = ctx;
+    call.t.keys[0] = r->keys;
+    call.t.keys[1] = s->keys;
+    call.t.pay[0] = r->payloads;
+    call.t.pay[1] = s->payloads;
+    call.t.hash[0] = call.t.hash[1] = nullptr;
+    call.t.rows[0] = (uint32_t)r->rows;
+    call.t.rows[1] = (uint32_t)s->rows;
+    call.t.joins = joins;
+    call.t.r_offsets = (const unsigned long long *)d_r_offsets;
+    call.t.s_offsets = (const unsigned long long *)d_s_offsets;
+    call.t.pair_offsets = (const unsigned long long *)d_pair_offsets;
+    call.t.pair_capacity = pair_capacity;
+    call.t.counts = (unsigned long long *)d_counts;
+    call.hs = spec_from(options, 1);
+    call.opt = options;
+    call.max_build_rows = max_build_rows && max_build_rows < r->rows ? max_build_rows : r->rows;
+    call.pairs = d_pairs;
+    call.status = d_status;
+    call.stream = st;
+    return dispatch(r->key_words, r->payload_bytes, 0, call);
+}
 
 extern "C" int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, vj_result *result, vj_stream_t stream) {
     VJ_CHECK(ctx && result, VJ_ERR_INVALID_ARGUMENT, "vj_join: null argument");

@@ -110,6 +110,12 @@ struct ProbeParams {
     uint64_t capacity;
     HashSpec hs;
     uint32_t *error;
+    // batches of joins (out_begin set): join j's probe rows start at s_join_begin[j]; its
+    // pairs go to out[out_begin[j], out_begin[j+1]), counted in out_counts[j]
+    uint32_t joins;
+    const uint32_t *s_join_begin;
+    const unsigned long long *out_begin;
+    unsigned long long *out_counts;
 };
 
 // ------------------------------------------------------------------ small helpers
@@ -688,6 +694,121 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q)
     }
 }
 
+// Output counter and range (first pair, capacity) of join j: its own for a batch of joins,
+// the whole output otherwise.
+template <typename QP>
+__device__ __forceinline__ unsigned long long *out_counter(const QP &Q, uint32_t j) {
+    return Q.out_begin ? Q.out_counts + j : Q.out_count;
+}
+template <typename QP>
+__device__ __forceinline__ void out_range(const QP &Q, uint32_t j, unsigned long long *first, unsigned long long *cap) {
+    if (Q.out_begin) {
+        *first = Q.out_begin[j];
+        *cap = Q.out_begin[j + 1] - Q.out_begin[j];
+    } else {
+        *first = 0;
+        *cap = Q.capacity;
+    }
+}
+
+// Join of a work item whose probe rows start at s0: the last join starting at or before it.
+__device__ __forceinline__ uint32_t join_of(const ProbeParams &Q, uint32_t s0) {
+    if (!Q.out_begin) return 0;
+    uint32_t lo = 0, hi = Q.joins - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (Q.s_join_begin[mid] <= s0) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- work items of a batch of joins
+//
+// Join j's build and probe rows after the pass are `parts` adjacent partitions on each side
+// (a single one without a pass). Small joins need fewer: adjacent partitions are grouped,
+// 2^k at a time, so a group holds about half a table of build rows -- rows of different
+// partitions never match, so one table may hold several. Each group gives
+// ceil(build rows / rcap) x ceil(probe rows / schunk) items.
+struct BatchGroups {
+    uint32_t groups, merge;
+};
+__device__ __forceinline__ BatchGroups batch_groups(const ProbeParams &Q, uint32_t parts, uint32_t j) {
+    const uint32_t nr = Q.r_end[(size_t)j * parts + parts - 1] - Q.r_begin[(size_t)j * parts];
+    const uint32_t half = Q.rcap / 2;
+    const uint32_t want = (nr + half - 1) / half;
+    uint32_t g = 1;
+    while (g < want && g < parts) g <<= 1;
+    return BatchGroups{g, parts / g};
+}
+__device__ __forceinline__ uint4 batch_group_rows(const ProbeParams &Q, uint32_t parts, uint32_t j, uint32_t g, uint32_t merge) {
+    const size_t p0 = (size_t)j * parts + (size_t)g * merge, p1 = p0 + merge - 1;
+    return make_uint4(Q.r_begin[p0], Q.r_end[p1], Q.s_begin[p0], Q.s_end[p1]);
+}
+__device__ __forceinline__ uint32_t batch_group_items(const ProbeParams &Q, const uint4 &d) {
+    if (d.y <= d.x || d.w <= d.z) return 0;
+    return ((d.y - d.x + Q.rcap - 1) / Q.rcap) * ((d.w - d.z + Q.schunk - 1) / Q.schunk);
+}
+
+// Grid: one block per join. COUNT: items of join j -> cnt[j]. !COUNT: its item
+// descriptors from base[j] on (none past item_cap).
+template <bool COUNT>
+__global__ void __launch_bounds__(256) batch_items_kernel(ProbeParams Q, uint32_t parts, uint32_t *cnt, const uint32_t *base) {
+    __shared__ uint32_t s_warp[32];
+    const uint32_t j = blockIdx.x;
+    const BatchGroups bg = batch_groups(Q, parts, j);
+    uint32_t run = COUNT ? 0u : base[j];
+    for (uint32_t g0 = 0; g0 < bg.groups; g0 += blockDim.x) {
+        const uint32_t g = g0 + threadIdx.x;
+        uint4 d = make_uint4(0, 0, 0, 0);
+        uint32_t n = 0;
+        if (g < bg.groups) {
+            d = batch_group_rows(Q, parts, j, g, bg.merge);
+            n = batch_group_items(Q, d);
+        }
+        uint32_t total = 0;
+        const uint32_t excl = block_exclusive_scan<uint32_t>(n, s_warp, &total);
+        if (!COUNT && n) {
+            uint32_t k = run + excl;
+            for (uint32_t r0 = d.x; r0 < d.y; r0 += Q.rcap) {
+                for (uint32_t s0 = d.z; s0 < d.w; s0 += Q.schunk) {
+                    if (k < Q.item_cap) Q.item_desc[k] = make_uint4(r0, min(d.y, r0 + Q.rcap), s0, min(d.w, s0 + Q.schunk));
+                    k++;
+                }
+            }
+        }
+        run += total;
+        __syncthreads();
+    }
+    if (COUNT && threadIdx.x == 0) cnt[j] = run;
+}
+
+// One block: item offset of every join, the item total, the counters reset. A batch with
+// more items than item_desc holds is refused (error flag 2, no items).
+__global__ void __launch_bounds__(PLAN_THREADS) batch_scan_kernel(ProbeParams Q, uint32_t *cnt_base) {
+    __shared__ unsigned long long s_warp[32];
+    const uint32_t per = (Q.joins + PLAN_THREADS - 1) / PLAN_THREADS;
+    const uint32_t j0 = threadIdx.x * per;
+    unsigned long long mine = 0;
+    for (uint32_t j = j0; j < j0 + per && j < Q.joins; j++) mine += cnt_base[j];
+    unsigned long long total = 0;
+    unsigned long long run = block_exclusive_scan<unsigned long long>(mine, s_warp, &total);
+    for (uint32_t j = j0; j < j0 + per && j < Q.joins; j++) {
+        const uint32_t c = cnt_base[j];
+        cnt_base[j] = (uint32_t)(run < 0xffffffffull ? run : 0xffffffffull);
+        run += c;
+        Q.out_counts[j] = 0;
+    }
+    if (threadIdx.x == 0) {
+        const bool fits = total <= Q.item_cap;
+        if (!fits) atomicOr(Q.error, 2u);
+        Q.item_begin[Q.np] = fits ? (uint32_t)total : 0u;
+        Q.item_begin[Q.np + 1] = 1u;
+        *Q.ticket = 0;
+        *Q.out_count = 0;
+    }
+}
+
 template <int PB>
 struct Pair;
 template <>
@@ -737,24 +858,28 @@ __device__ __forceinline__ uint4 item_rows(const ProbeParams &Q, uint32_t it, bo
 // filled before it, and switch buffers. The atomic's latency overlaps a sub-chunk of work.
 template <int PB, typename QP>
 __device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
-                                             unsigned long long *pend_base) {
+                                             unsigned long long *pend_base, uint32_t join, uint32_t *pend_join, uint32_t *flush_join) {
     using PT = typename Pair<PB>::T;
     __syncthreads();
     if (threadIdx.x == 0) {
         *flush_base = *pend_base;
         *flush_n = *pend_n;
+        *flush_join = *pend_join;
         const uint32_t n = min(*out_n, Q.outcap);
         *pend_n = n;
-        if (n) *pend_base = atomicAdd(Q.out_count, (unsigned long long)n);
+        *pend_join = join;
+        if (n) *pend_base = atomicAdd(out_counter(Q, join), (unsigned long long)n);
         *out_n = 0;
     }
     __syncthreads();
     const uint32_t n = *flush_n;
+    unsigned long long first, cap;
+    out_range(Q, *flush_join, &first, &cap);
     const unsigned long long base = *flush_base;
     const PT *src = stage0 + (size_t)(cur ^ 1) * Q.outcap;
-    PT *out = (PT *)Q.out;
+    PT *out = (PT *)Q.out + first;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        if (base + i < Q.capacity) __stcs(out + base + i, src[i]);
+        if (base + i < cap) __stcs(out + base + i, src[i]);
     }
     cur ^= 1;
 }
@@ -776,6 +901,8 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
 
     __shared__ uint32_t s_item, s_next_item;
     __shared__ uint4 s_rows, s_next_rows;
+    __shared__ uint32_t s_join, s_next_join;    // batches of joins: the item's join
+    __shared__ uint32_t s_pend_join, s_flush_join;
     __shared__ uint32_t s_out_n;                 // pairs staged in the current buffer
     __shared__ uint32_t s_flush_n;               // pairs of the other buffer awaiting copy-out
     __shared__ unsigned long long s_flush_base;  // their output position
@@ -796,6 +923,9 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         s_flush_n = 0;
         s_pend_base = 0;
         s_pend_n = 0;
+        s_pend_join = 0;
+        s_flush_join = 0;
+        s_next_join = 0;
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_init(&bar[2], 1);
@@ -804,6 +934,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         if (s_next_item < total_items) {
             const uint4 d = item_rows(Q, s_next_item, direct);
             s_next_rows = d;
+            s_next_join = join_of(Q, d.z);
             C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
             C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
         }
@@ -817,12 +948,14 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         if (threadIdx.x == 0) {
             s_item = s_next_item;
             s_rows = s_next_rows;
+            s_join = s_next_join;
             s_dups = 0;
             if (s_item < total_items) {
                 s_next_item = atomicAdd(Q.ticket, 1u);
                 if (s_next_item < total_items) {
                     const uint4 d = item_rows(Q, s_next_item, direct);
                     s_next_rows = d;
+                    s_next_join = join_of(Q, d.z);
                     C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
                     C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
                 }
@@ -833,6 +966,9 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         if (item >= total_items) break;
         const uint4 d = s_rows;
         const uint32_t r0 = d.x, r1 = d.y, s0 = d.z, s1 = d.w;
+        const uint32_t join = s_join;
+        unsigned long long o_first, o_cap;  // this item's output range (overflow writes)
+        out_range(Q, join, &o_first, &o_cap);
         const uint32_t nr = r1 - r0;
         const uint32_t nsub = (s1 - s0 + Q.sub_rows - 1) / Q.sub_rows;
         uint32_t cap = 64;
@@ -960,8 +1096,8 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                             if (pos < Q.outcap) {
                                 stage[pos] = pr;
                             } else {
-                                const unsigned long long g = atomicAdd(Q.out_count, 1ull);
-                                if (g < Q.capacity) ((PT *)Q.out)[g] = pr;
+                                const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
                             }
                         }
                         if (m1 >= 0) {
@@ -970,8 +1106,8 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                             if (pos < Q.outcap) {
                                 stage[pos] = pr;
                             } else {
-                                const unsigned long long g = atomicAdd(Q.out_count, 1ull);
-                                if (g < Q.capacity) ((PT *)Q.out)[g] = pr;
+                                const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
                             }
                         }
                     }
@@ -1020,20 +1156,20 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                                     stage[pos] = Pair<PB>::make(rp, sp);
                                 } else {
                                     // staging full (build rows with many duplicates): direct write
-                                    const unsigned long long g = atomicAdd(Q.out_count, 1ull);
-                                    if (g < Q.capacity) ((PT *)Q.out)[g] = Pair<PB>::make(rp, sp);
+                                    const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                    if (g < o_cap) ((PT *)Q.out)[o_first + g] = Pair<PB>::make(rp, sp);
                                 }
                             }
                         }
                     }
                 }
             }
-            rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
+            rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, join, &s_pend_join, &s_flush_join);
         }
     }
     // drain: the buffer filled last and the one before it
-    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
-    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base);
+    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
+    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
 }
 
 }  // namespace vj

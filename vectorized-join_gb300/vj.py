@@ -58,6 +58,7 @@ EXPORTS = [
     "vj_partition_noalloc",
     "vj_build_probe",
     "vj_join",
+    "vj_join_batch",
     "vj_join_host",
     "vj_result_free",
     "vj_pairs_digest",
@@ -188,6 +189,8 @@ def load() -> ctypes.CDLL:
         L.vj_build_probe.argtypes = [vp, ctypes.POINTER(VjTable), vp, ctypes.POINTER(VjTable), vp, i32, i32, vp, u64, ctypes.POINTER(u64), vp]
         L.vj_join.restype = i32
         L.vj_join.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), ctypes.POINTER(VjResult), vp]
+        L.vj_join_batch.restype = i32
+        L.vj_join_batch.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.c_uint32, vp, vp, u64, ctypes.POINTER(VjJoinOptions), vp, vp, u64, vp, vp, vp]
         L.vj_join_host.restype = i32
         L.vj_join_host.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), vp, u64, ctypes.POINTER(u64), vp]
         L.vj_result_free.restype = i32
@@ -324,6 +327,16 @@ class Context:
 
     def free(self, res: VjResult) -> None:
         check(self.lib.vj_result_free(self.handle, ctypes.byref(res)))
+
+    def join_batch(self, r: VjTable, s: VjTable, joins: int, r_offsets, s_offsets, pairs, pair_offsets, pair_capacity: int, counts, status=None, max_build_rows: int = 0, opts: VjJoinOptions | None = None, stream=None) -> None:
+        """vj_join_batch: `joins` independent joins in one launch sequence (asynchronous).
+        Offsets, counts and status are device arrays (u64 offsets of joins + 1 entries)."""
+        check(
+            self.lib.vj_join_batch(
+                self.handle, ctypes.byref(r), ctypes.byref(s), joins, ptr(r_offsets), ptr(s_offsets), max_build_rows, ctypes.byref(opts) if opts else None, ptr(pairs), ptr(pair_offsets), pair_capacity,
+                ptr(counts), ptr(status), stream_handle(stream)
+            )
+        )
 
     def join_host(self, r: VjTable, s: VjTable, out, capacity: int, opts: VjJoinOptions | None = None, stream=None) -> int:
         n = u64(0)
