@@ -431,6 +431,101 @@ def run_skew_join(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_batch_join(args) -> None:
+    """4096 independent int32 joins, |R_i| log-uniform over [2^10, 2^20], |S_i| = 4 |R_i|,
+    75% of S_i drawn from R_i (per-join seed = 42 + i): one vj_join_batch call replayed from
+    a CUDA graph, against the same 4096 joins as sequential vj_join calls."""
+    import numpy as np
+    import torch
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    joins = 4096
+    rng = np.random.default_rng(SEED)
+    r_sizes = np.exp(rng.uniform(np.log(2.0**10), np.log(2.0**20), size=joins)).astype(np.int64)
+    s_sizes = 4 * r_sizes
+    r_off = np.concatenate([[0], np.cumsum(r_sizes)]).astype(np.int64)
+    s_off = np.concatenate([[0], np.cumsum(s_sizes)]).astype(np.int64)
+    nr, ns = int(r_off[-1]), int(s_off[-1])
+    rk = torch.empty(nr, dtype=torch.int32, device=dev)
+    rp = torch.empty_like(rk)
+    sk = torch.empty(ns, dtype=torch.int32, device=dev)
+    sp = torch.empty_like(sk)
+    thr = int(round(0.75 * (1 << 32)))
+    for j in range(joins):
+        a, b, c, d = int(r_off[j]), int(r_off[j + 1]), int(s_off[j]), int(s_off[j + 1])
+        vj.generate_join(SEED + j, 4, 4, b - a, d - c, thr, rk[a:b], rp[a:b], sk[c:d], sp[c:d])
+    want = [vj.generate_join_expect(SEED + j, int(r_sizes[j]), int(s_sizes[j]), thr) for j in range(joins)]
+    m = sum(w[0] for w in want)
+    p_off = s_off.copy()  # join j may emit up to |S_j| pairs (unique build keys)
+    pairs = torch.empty((ns, 2), dtype=torch.int32, device=dev)
+    counts = torch.zeros(joins, dtype=torch.int64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    d_r = torch.from_numpy(r_off).to(dev)
+    d_s = torch.from_numpy(s_off).to(dev)
+    d_p = torch.from_numpy(p_off).to(dev)
+    ctx = vj.Context(0)
+    t_r, t_s = vj.table(rk, rp, nr, 1, 4), vj.table(sk, sp, ns, 1, 4)
+    stream = torch.cuda.Stream()
+    call = lambda: ctx.join_batch(t_r, t_s, joins, d_r, d_s, pairs, d_p, ns, counts, status, max_build_rows=int(r_sizes.max()), stream=stream)
+    call()  # grows the workspace outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        call()
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got = counts.cpu().numpy()
+    for j in range(joins):
+        assert got[j] == want[j][0], j
+        assert vj.pairs_digest(pairs[int(p_off[j]) :], int(got[j]), 4) == (want[j][1], want[j][2]), j
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = _timed(torch, torch.cuda.current_stream(), g.replay, args.steps, args.warmup)  # replay() launches on the current stream
+    clocks = sampler.stop()
+    t_batch = sum(ms) / len(ms)
+    # the same joins back to back through vj_join (each synchronises to return its count)
+    seq_stream = torch.cuda.current_stream()
+
+    def sequential():
+        for j in range(joins):
+            a, b, c, d = int(r_off[j]), int(r_off[j + 1]), int(s_off[j]), int(s_off[j + 1])
+            res = ctx.join(vj.table(rk[a:b], rp[a:b], b - a, 1, 4), vj.table(sk[c:d], sp[c:d], d - c, 1, 4), out=pairs[c:d], capacity=d - c, stream=seq_stream)
+            assert res.count == want[j][0]
+
+    sequential()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(seq_stream)
+    sequential()
+    e1.record(seq_stream)
+    torch.cuda.synchronize()
+    t_seq = e0.elapsed_time(e1)
+    n = nr + ns
+    b_alg = n * (1 * (4 + 2 * 8) + 8) + m * 2 * 4
+    peak, src = measured_peak()
+    cfg = {
+        "workload": "batched join: 4096 int32 joins, |R_i| log-uniform [2^10, 2^20], |S_i| = 4|R_i|, 75% match, one vj_join_batch in a CUDA graph",
+        "joins": joins,
+        "r_rows": nr,
+        "s_rows": ns,
+        "l2_policy": "inputs (%.1f GiB) larger than L2" % (n * 8 / 2**30),
+    }
+    line = _base_line(METRIC, n / (t_batch / 1000), UNIT, args.steps, args.warmup, t_batch, "int32", cfg)
+    line["join_roofline"] = {"bytes_alg_per_join": b_alg, "achieved": b_alg / (t_batch / 1000) / 1e9, "peak": peak, "unit": "GB/s", "frac": b_alg / (t_batch / 1000) / 1e9 / peak, "peak_source": src, "passes": 1}
+    line["latency_ms"] = _latency(ms)
+    line["sequential"] = {"ms": t_seq, "value": n / (t_seq / 1000), "unit": UNIT, "api": "4096 vj_join calls back to back"}
+    line["speedup_vs_sequential"] = t_seq / t_batch
+    line["matches"] = m
+    line["clocks"] = clocks
+    print(json.dumps(line), flush=True)
+
+
 def run_hash_bench(args) -> None:
     """hash_func over 2^30 keys of 8, 16 and 32 uniform random bytes, FNV-1a 64 and the
     custom hash (custom_xor_hw), 64-bit chunks. Bytes = n * (key bytes + 8)."""
@@ -489,11 +584,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
+    ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "join-batch", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "ours" and args.workload != "join":
-        {"join-small": run_small_join, "join-skew": run_skew_join, "hash": run_hash_bench}[args.workload](args)
+        {"join-small": run_small_join, "join-skew": run_skew_join, "join-batch": run_batch_join, "hash": run_hash_bench}[args.workload](args)
         return
     if args.small:
         args.shift = max(args.shift, 3)

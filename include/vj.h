@@ -262,7 +262,7 @@ VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
  * vj_join_batch -- many independent joins in one launch sequence. The reference runs one
  * JoinProvider::join per call; its nearest counterpart is the bucket-pair work list of a
  * single join (src/join/join_provider.cuh:717-795).
- * Join j joins build rows [d_r_offsets[j], d_r_offsets[j+1]) of r with probe rows
+ * joins: 1..16384. Join j joins build rows [d_r_offsets[j], d_r_offsets[j+1]) of r with probe rows
  * [d_s_offsets[j], d_s_offsets[j+1]) of s (device arrays of joins + 1 uint64_t, starting
  * at 0, ending at the table's rows, non-decreasing). Its pairs (r payload, s payload) go to
  * d_pairs[d_pair_offsets[j] .. d_pair_offsets[j+1]) (pair_capacity pairs in all) and their

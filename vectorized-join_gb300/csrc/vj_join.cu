@@ -243,10 +243,10 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
     return VJ_OK;
 }
 
-template <int KW, int PB, int HS, bool AOS>
+template <int KW, int PB, int HS, bool AOS, bool BATCH>
 int probe_grid(const DeviceInfo &info, int threads, size_t smem, int *grid) {
     int per_sm = 0;
-    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS>, threads, smem));
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS, BATCH>, threads, smem));
     if (per_sm < 1) per_sm = 1;
     *grid = info.sms * per_sm;
     return VJ_OK;
@@ -316,6 +316,7 @@ struct JoinRun {
     size_t probe_smem;
     int probe_grid;
     // batches of joins: per-join item counts, partitions per join
+    bool batch = false;
     uint32_t *batch_cnt = nullptr;
     uint32_t batch_parts = 1;
     // L2-table build/probe (tables == VJ_TABLES_L2)
@@ -337,13 +338,14 @@ int l2_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     return VJ_OK;
 }
 
-template <int KW, int PB, int HS, bool AOS>
+template <int KW, int PB, int HS, bool AOS, bool BATCH>
 int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     run->aos = AOS;
+    run->batch = BATCH;
     run->threads = pl.threads;
     run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
-    VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS>, run->probe_smem));
-    return probe_grid<KW, PB, HS, AOS>(ctx->info, pl.threads, run->probe_smem, &run->probe_grid);
+    VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS, BATCH>, run->probe_smem));
+    return probe_grid<KW, PB, HS, AOS, BATCH>(ctx->info, pl.threads, run->probe_smem, &run->probe_grid);
 }
 
 // Everything up to (not including) the probe launch. Returns probe parameters whose
@@ -539,9 +541,9 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         return l2_setup<KW, PB, HS>(ctx, pl, run);
     }
     if (pl.passes == 0) {
-        return probe_setup<KW, PB, HS, false>(ctx, pl, run);
+        return batch ? probe_setup<KW, PB, HS, false, true>(ctx, pl, run) : probe_setup<KW, PB, HS, false, false>(ctx, pl, run);
     }
-    return probe_setup<KW, PB, HS, true>(ctx, pl, run);
+    return batch ? probe_setup<KW, PB, HS, true, true>(ctx, pl, run) : probe_setup<KW, PB, HS, true, false>(ctx, pl, run);
 }
 
 template <int KW, int PB, int HS>
@@ -576,9 +578,11 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         VJ_CUDA(cudaGetLastError());
     }
     if (run.aos) {
-        probe_kernel<KW, PB, HS, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
+        if (run.batch) probe_kernel<KW, PB, HS, true, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
+        else probe_kernel<KW, PB, HS, true, false><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     } else {
-        probe_kernel<KW, PB, HS, false><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
+        if (run.batch) probe_kernel<KW, PB, HS, false, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
+        else probe_kernel<KW, PB, HS, false, false><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     }
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_PROBE_END, stream);
@@ -935,7 +939,8 @@ extern "C" int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, 
     VJ_TRY(check_table(r, "vj_join_batch: r"));
     VJ_TRY(check_table(s, "vj_join_batch: s"));
     VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: r and s must have the same key_words and payload_bytes");
-    VJ_CHECK(joins >= 1 && joins <= (1u << 22), VJ_ERR_UNSUPPORTED, "vj_join_batch: joins must be in [1, 2^22] (got %u)", joins);
+    // the pass's unit scan keeps one shared-memory word per unit, two units per join at least
+    VJ_CHECK(joins >= 1 && joins <= 16384, VJ_ERR_UNSUPPORTED, "vj_join_batch: joins must be in [1, 16384] (got %u)", joins);
     VJ_CHECK(d_r_offsets && d_s_offsets && d_pair_offsets && d_counts, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null offsets or counts");
     VJ_CHECK(d_pairs != nullptr || pair_capacity == 0, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null output with capacity > 0");
     VJ_CUDA(cudaSetDevice(ctx->device));

@@ -696,13 +696,14 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q)
 
 // Output counter and range (first pair, capacity) of join j: its own for a batch of joins,
 // the whole output otherwise.
-template <typename QP>
+template <bool BATCH, typename QP>
 __device__ __forceinline__ unsigned long long *out_counter(const QP &Q, uint32_t j) {
-    return Q.out_begin ? Q.out_counts + j : Q.out_count;
+    if constexpr (BATCH) return Q.out_counts + j;
+    else return Q.out_count;
 }
-template <typename QP>
+template <bool BATCH, typename QP>
 __device__ __forceinline__ void out_range(const QP &Q, uint32_t j, unsigned long long *first, unsigned long long *cap) {
-    if (Q.out_begin) {
+    if constexpr (BATCH) {
         *first = Q.out_begin[j];
         *cap = Q.out_begin[j + 1] - Q.out_begin[j];
     } else {
@@ -856,7 +857,7 @@ __device__ __forceinline__ uint4 item_rows(const ProbeParams &Q, uint32_t it, bo
 // End of a probe sub-chunk (all threads): reserve the output range of the buffer just
 // filled (one atomic, whose result is read one sub-chunk later), copy out the buffer
 // filled before it, and switch buffers. The atomic's latency overlaps a sub-chunk of work.
-template <int PB, typename QP>
+template <int PB, bool BATCH, typename QP>
 __device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
                                              unsigned long long *pend_base, uint32_t join, uint32_t *pend_join, uint32_t *flush_join) {
     using PT = typename Pair<PB>::T;
@@ -864,17 +865,17 @@ __device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *
     if (threadIdx.x == 0) {
         *flush_base = *pend_base;
         *flush_n = *pend_n;
-        *flush_join = *pend_join;
+        if constexpr (BATCH) *flush_join = *pend_join;
         const uint32_t n = min(*out_n, Q.outcap);
         *pend_n = n;
-        *pend_join = join;
-        if (n) *pend_base = atomicAdd(out_counter(Q, join), (unsigned long long)n);
+        if constexpr (BATCH) *pend_join = join;
+        if (n) *pend_base = atomicAdd(out_counter<BATCH>(Q, join), (unsigned long long)n);
         *out_n = 0;
     }
     __syncthreads();
     const uint32_t n = *flush_n;
     unsigned long long first, cap;
-    out_range(Q, *flush_join, &first, &cap);
+    out_range<BATCH>(Q, BATCH ? *flush_join : 0u, &first, &cap);
     const unsigned long long base = *flush_base;
     const PT *src = stage0 + (size_t)(cur ^ 1) * Q.outcap;
     PT *out = (PT *)Q.out + first;
@@ -884,7 +885,8 @@ __device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *
     cur ^= 1;
 }
 
-template <int KW, int PB, int HS, bool AOS>
+// BATCH: a batch of joins, each item's pairs go to its join's output range.
+template <int KW, int PB, int HS, bool AOS, bool BATCH>
 __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
     using C = Chunk<KW, PB, HS, AOS>;
     using Pt = typename PayloadType<PB>::T;
@@ -934,7 +936,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         if (s_next_item < total_items) {
             const uint4 d = item_rows(Q, s_next_item, direct);
             s_next_rows = d;
-            s_next_join = join_of(Q, d.z);
+            if constexpr (BATCH) s_next_join = join_of(Q, d.z);
             C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
             C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
         }
@@ -955,7 +957,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                 if (s_next_item < total_items) {
                     const uint4 d = item_rows(Q, s_next_item, direct);
                     s_next_rows = d;
-                    s_next_join = join_of(Q, d.z);
+                    if constexpr (BATCH) s_next_join = join_of(Q, d.z);
                     C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
                     C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
                 }
@@ -966,9 +968,9 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
         if (item >= total_items) break;
         const uint4 d = s_rows;
         const uint32_t r0 = d.x, r1 = d.y, s0 = d.z, s1 = d.w;
-        const uint32_t join = s_join;
+        const uint32_t join = BATCH ? s_join : 0u;
         unsigned long long o_first, o_cap;  // this item's output range (overflow writes)
-        out_range(Q, join, &o_first, &o_cap);
+        out_range<BATCH>(Q, join, &o_first, &o_cap);
         const uint32_t nr = r1 - r0;
         const uint32_t nsub = (s1 - s0 + Q.sub_rows - 1) / Q.sub_rows;
         uint32_t cap = 64;
@@ -1096,7 +1098,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                             if (pos < Q.outcap) {
                                 stage[pos] = pr;
                             } else {
-                                const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
                                 if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
                             }
                         }
@@ -1106,7 +1108,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                             if (pos < Q.outcap) {
                                 stage[pos] = pr;
                             } else {
-                                const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
                                 if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
                             }
                         }
@@ -1156,7 +1158,7 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                                     stage[pos] = Pair<PB>::make(rp, sp);
                                 } else {
                                     // staging full (build rows with many duplicates): direct write
-                                    const unsigned long long g = atomicAdd(out_counter(Q, join), 1ull);
+                                    const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
                                     if (g < o_cap) ((PT *)Q.out)[o_first + g] = Pair<PB>::make(rp, sp);
                                 }
                             }
@@ -1164,12 +1166,12 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
                     }
                 }
             }
-            rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, join, &s_pend_join, &s_flush_join);
+            rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, join, &s_pend_join, &s_flush_join);
         }
     }
     // drain: the buffer filled last and the one before it
-    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
-    rotate_stage<PB>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
+    rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
+    rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
 }
 
 }  // namespace vj
