@@ -278,6 +278,48 @@ VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
 VJ_API int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, uint32_t joins, const uint64_t *d_r_offsets, const uint64_t *d_s_offsets, uint64_t max_build_rows,
                          const vj_join_options *options, void *d_pairs, const uint64_t *d_pair_offsets, uint64_t pair_capacity, uint64_t *d_counts, uint32_t *d_status, vj_stream_t stream);
 
+/*
+ * Join server -- the serving form of the join: requests of different sizes arrive over
+ * time, are admitted while the memory held by running joins stays within a budget, and
+ * run concurrently (one context and stream per slot, whose partition buffers stay
+ * resident between requests). The reference bounds memory and concurrency inside a single
+ * join (DeviceConfig::reserve_memory, src/join/join_provider.cuh:138-150; its probe-thread
+ * semaphore and stream pool, :453-480, :534-560); here the unit is a whole request.
+ *   vj_server_create: `slots` concurrent joins (1..64) under memory_budget_bytes (0 = the
+ *     device's free memory at creation).
+ *   vj_server_submit: queue a join of DEVICE tables r and s; its pairs go to the caller's
+ *     d_pairs (capacity pairs). Tables and output must stay valid until the request is
+ *     waited for. A join whose estimated footprint exceeds the whole budget is refused
+ *     with VJ_ERR_BUDGET. Admission is in arrival order, except that a request that fits
+ *     may pass a head that does not (at most 8 times per head).
+ *   vj_server_wait: block until the request is done; its status is vj_join's (VJ_OK, or
+ *     VJ_ERR_CAPACITY with count = pairs needed), times are seconds since the server
+ *     started. Each request's result equals vj_join's on the same tables.
+ *   vj_server_destroy: finishes every queued request, then frees the slots.
+ */
+typedef struct vj_server vj_server;
+typedef struct vj_request_result {
+    int32_t status;
+    int32_t slot;       /* slot that ran it */
+    uint64_t count;     /* pairs of the join */
+    double submit_s;    /* submitted, started, finished: seconds since the server started */
+    double start_s;
+    double finish_s;
+} vj_request_result;
+typedef struct vj_server_stats {
+    uint64_t submitted;
+    uint64_t completed;
+    uint64_t peak_bytes;  /* largest sum of the bytes the slots held or had reserved */
+    uint64_t budget;
+    int32_t peak_running; /* most requests running at once */
+    int32_t slots;
+} vj_server_stats;
+VJ_API int vj_server_create(int device, uint64_t memory_budget_bytes, int slots, vj_server **out);
+VJ_API int vj_server_submit(vj_server *srv, const vj_table *r, const vj_table *s, const vj_join_options *options, void *d_pairs, uint64_t capacity, uint64_t *request_id);
+VJ_API int vj_server_wait(vj_server *srv, uint64_t request_id, vj_request_result *out);
+VJ_API int vj_server_stats_get(vj_server *srv, vj_server_stats *out);
+VJ_API int vj_server_destroy(vj_server *srv);
+
 /* Order-independent digest of a pair list: sum and xor of a 64-bit mix of each pair, the
  * same function the CPU oracle computes. For comparing full-size joins without sorting.
  * Synchronises stream. */

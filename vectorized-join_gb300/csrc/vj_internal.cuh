@@ -419,4 +419,6 @@ void profile_mark(vj_ctx *ctx, int mark, cudaStream_t stream);
 int workspace_reserve(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
 int owned_alloc(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
 void owned_release(vj_ctx *ctx, size_t bytes);
+// Upper estimate of the device bytes a vj_join of r and s takes from a context.
+int join_footprint(const vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *opt, uint64_t *bytes);
 }  // namespace vj

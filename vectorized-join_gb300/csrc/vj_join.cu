@@ -927,7 +927,33 @@ struct BatchCall {
     }
 };
 
+struct FootprintCall {
+    const vj_ctx *ctx;
+    uint64_t nr, ns;
+    const vj_join_options *opt;
+    uint64_t *bytes;
+    template <int KW, int PB, int HS>
+    int run() {
+        const Plan pl = make_plan<KW, PB, HS>(nr, ns, ctx->info, opt);
+        using L = Layout<KW, PB, HS>;
+        // partition buffers of every pass (grown by an eighth), bookkeeping, owned output of |S| pairs
+        const uint64_t bufs = (uint64_t)pl.passes * (nr + ns) * L::STRIDE;
+        *bytes = bufs + bufs / 8 + ns * 2 * PB + (64ull << 20);
+        return VJ_OK;
+    }
+};
+
 }  // namespace
+
+// Device bytes a vj_join of these tables takes from a context: its workspace (partition
+// buffers and bookkeeping) and a library-owned output of |S| pairs -- an upper estimate
+// for admission by memory budget.
+int join_footprint(const vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *opt, uint64_t *bytes) {
+    VJ_TRY(check_table(r, "join_footprint: r"));
+    VJ_TRY(check_table(s, "join_footprint: s"));
+    FootprintCall call{ctx, r->rows, s->rows, opt, bytes};
+    return dispatch(r->key_words, r->payload_bytes, 0, call);
+}
 
 }  // namespace vj
 

@@ -59,6 +59,11 @@ EXPORTS = [
     "vj_build_probe",
     "vj_join",
     "vj_join_batch",
+    "vj_server_create",
+    "vj_server_submit",
+    "vj_server_wait",
+    "vj_server_stats_get",
+    "vj_server_destroy",
     "vj_join_host",
     "vj_result_free",
     "vj_pairs_digest",
@@ -139,6 +144,28 @@ class VjProfile(ctypes.Structure):
         }
 
 
+class VjRequestResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("slot", ctypes.c_int32),
+        ("count", ctypes.c_uint64),
+        ("submit_s", ctypes.c_double),
+        ("start_s", ctypes.c_double),
+        ("finish_s", ctypes.c_double),
+    ]
+
+
+class VjServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("peak_bytes", ctypes.c_uint64),
+        ("budget", ctypes.c_uint64),
+        ("peak_running", ctypes.c_int32),
+        ("slots", ctypes.c_int32),
+    ]
+
+
 class VjError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"vj status {status}: {message}")
@@ -191,6 +218,16 @@ def load() -> ctypes.CDLL:
         L.vj_join.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), ctypes.POINTER(VjResult), vp]
         L.vj_join_batch.restype = i32
         L.vj_join_batch.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.c_uint32, vp, vp, u64, ctypes.POINTER(VjJoinOptions), vp, vp, u64, vp, vp, vp]
+        L.vj_server_create.restype = i32
+        L.vj_server_create.argtypes = [i32, u64, i32, ctypes.POINTER(vp)]
+        L.vj_server_submit.restype = i32
+        L.vj_server_submit.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), vp, u64, ctypes.POINTER(u64)]
+        L.vj_server_wait.restype = i32
+        L.vj_server_wait.argtypes = [vp, u64, ctypes.POINTER(VjRequestResult)]
+        L.vj_server_stats_get.restype = i32
+        L.vj_server_stats_get.argtypes = [vp, ctypes.POINTER(VjServerStats)]
+        L.vj_server_destroy.restype = i32
+        L.vj_server_destroy.argtypes = [vp]
         L.vj_join_host.restype = i32
         L.vj_join_host.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), vp, u64, ctypes.POINTER(u64), vp]
         L.vj_result_free.restype = i32
@@ -392,3 +429,36 @@ def generate_join_expect(seed: int, nr: int, ns: int, match_threshold: int, stre
     x = u64(0)
     check(load().vj_generate_join_expect(seed, nr, ns, match_threshold, ctypes.byref(c), ctypes.byref(s), ctypes.byref(x), stream_handle(stream)))
     return int(c.value), int(s.value), int(x.value)
+
+
+class Server:
+    """vj_server wrapper: submit joins of device tables, wait for their results."""
+
+    def __init__(self, device: int = 0, budget: int = 0, slots: int = 4):
+        self.lib = load()
+        h = vp()
+        check(self.lib.vj_server_create(device, budget, slots, ctypes.byref(h)))
+        self.handle = h
+        self._keep: dict[int, tuple] = {}
+
+    def submit(self, r: VjTable, s: VjTable, out, capacity: int, opts: VjJoinOptions | None = None) -> int:
+        rid = u64(0)
+        check(self.lib.vj_server_submit(self.handle, ctypes.byref(r), ctypes.byref(s), ctypes.byref(opts) if opts else None, ptr(out), capacity, ctypes.byref(rid)))
+        self._keep[int(rid.value)] = (r, s, out, opts)  # buffers live until the wait
+        return int(rid.value)
+
+    def wait(self, rid: int) -> VjRequestResult:
+        res = VjRequestResult()
+        check(self.lib.vj_server_wait(self.handle, rid, ctypes.byref(res)))
+        self._keep.pop(rid, None)
+        return res
+
+    def stats(self) -> VjServerStats:
+        st = VjServerStats()
+        check(self.lib.vj_server_stats_get(self.handle, ctypes.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if self.handle:
+            check(self.lib.vj_server_destroy(self.handle))
+            self.handle = None
