@@ -526,6 +526,105 @@ def run_batch_join(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args) -> None:
+    """Serving loop: 120 join requests, int64 keys, |R| log-uniform over [2^12, 2^24],
+    |S| = U{2..8} |R|, match ratio U[0.1, 1.0], probe keys uniform or Zipf(0.8) over R
+    (50/50), arriving as a Poisson process; the server admits them into 4 slots under a
+    150 GB budget. Compared with the serialized loop (one slot) on the same arrivals; every
+    request's pairs digest must be the same in both."""
+    import numpy as np
+    import torch
+
+    graft = _import(ROOT / "__graft_entry__.py", "graft_entry")
+    graft.build()
+    vj = _import(PKG / "vj.py", "vj")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(SEED)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    n_req = 120
+    reqs = []
+    tuples = 0
+    for i in range(n_req):
+        nr = int(np.exp(rng.uniform(np.log(2.0**12), np.log(2.0**24))))
+        ns = int(rng.integers(2, 9)) * nr
+        ratio = float(rng.uniform(0.1, 1.0))
+        zipf = bool(rng.random() < 0.5)
+        rk = torch.empty(nr, dtype=torch.int64, device=dev)
+        rp = torch.empty_like(rk)
+        sk = torch.empty(ns, dtype=torch.int64, device=dev)
+        sp = torch.empty_like(sk)
+        vj.generate_join(SEED + i, 8, 8, nr, ns, int(ratio * (1 << 32)), rk, rp, sk, sp)
+        if zipf:  # hits drawn Zipf(0.8) over R (inverse of the continuous CDF), misses random
+            u = torch.rand(ns, dtype=torch.float64, generator=gen, device=dev)
+            rank = torch.floor(((nr ** 0.2 - 1.0) * u + 1.0) ** 5.0).to(torch.int64).clamp_(1, nr) - 1
+            perm = torch.randperm(nr, generator=gen, device=dev)
+            hit = torch.rand(ns, generator=gen, device=dev) < ratio
+            miss = torch.randint(-(2**62), 2**62, (ns,), generator=gen, device=dev, dtype=torch.int64)
+            sk = torch.where(hit, rk[perm[rank]], miss)
+            del u, rank, perm, hit, miss
+        out = torch.empty((ns, 2), dtype=torch.int64, device=dev)
+        reqs.append((vj.table(rk, rp, nr, 2, 8), vj.table(sk, sp, ns, 2, 8), out, ns))
+        tuples += nr + ns
+    torch.cuda.synchronize()
+
+    def serve(slots: int, arrivals):
+        srv = vj.Server(0, 150 << 30, slots)
+        try:
+            t0 = time.perf_counter()
+            ids = []
+            for (r, s_, out, cap), at in zip(reqs, arrivals):
+                while time.perf_counter() - t0 < at:
+                    pass
+                ids.append(srv.submit(r, s_, out, cap))
+            res = [srv.wait(i) for i in ids]
+            st = srv.stats()
+        finally:
+            srv.close()
+        assert all(x.status == 0 for x in res)
+        lat = sorted((x.finish_s - x.submit_s) * 1000 for x in res)
+        span = max(x.finish_s for x in res) - min(x.submit_s for x in res)
+        digests = [vj.pairs_digest(q[2], x.count, 8) for q, x in zip(reqs, res)]
+        return {
+            "tuples_per_s": tuples / span,
+            "makespan_s": span,
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))], "max": lat[-1]},
+            "peak_running": st.peak_running,
+            "peak_gb": st.peak_bytes / 1e9,
+        }, [x.count for x in res], digests
+
+    zero = [0.0] * n_req
+    serve(4, zero)  # warm-up: contexts, workspaces, module loading
+    sat_ser, counts_ser, dig_ser = serve(1, zero)
+    sat_srv, counts_srv, dig_srv = serve(4, zero)
+    assert counts_ser == counts_srv and dig_ser == dig_srv, "a result differs between the serialized loop and the server"
+    mu = n_req / sat_ser["makespan_s"]  # serialized service rate, requests / s
+    loads = []
+    sampler = ClockSampler(0)
+    sampler.start()
+    for frac in (0.5, 0.9, 2.0):
+        lam = frac * mu
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n_req))
+        arrivals -= arrivals[0]
+        srv_r, c1, d1 = serve(4, arrivals)
+        ser_r, c2, d2 = serve(1, arrivals)
+        assert c1 == counts_ser and c2 == counts_ser and d1 == dig_ser and d2 == dig_ser
+        loads.append({"offered_load_of_serial_rate": frac, "rate_req_per_s": lam, "server": srv_r, "serialized": ser_r})
+    clocks = sampler.stop()
+    cfg = {
+        "workload": "serving loop: 120 int64 join requests, |R| log-uniform [2^12, 2^24], |S| = U{2..8}|R|, match U[0.1,1], keys uniform or Zipf(0.8), Poisson arrivals, 150 GB budget, 4 slots",
+        "requests": n_req,
+        "tuples": tuples,
+        "l2_policy": "request tables (%.1f GiB in all) larger than L2" % (tuples * 16 / 2**30),
+    }
+    line = _base_line(METRIC, sat_srv["tuples_per_s"], UNIT, 1, 1, sat_srv["makespan_s"] * 1000, "int64", cfg)
+    line["saturation"] = {"server": sat_srv, "serialized": sat_ser, "speedup": sat_ser["makespan_s"] / sat_srv["makespan_s"]}
+    line["loads"] = loads
+    line["clocks"] = clocks
+    print(json.dumps(line), flush=True)
+
+
 def run_hash_bench(args) -> None:
     """hash_func over 2^30 keys of 8, 16 and 32 uniform random bytes, FNV-1a 64 and the
     custom hash (custom_xor_hw), 64-bit chunks. Bytes = n * (key bytes + 8)."""
@@ -584,11 +683,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "join-batch", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
+    ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "join-batch", "serve", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "ours" and args.workload != "join":
-        {"join-small": run_small_join, "join-skew": run_skew_join, "join-batch": run_batch_join, "hash": run_hash_bench}[args.workload](args)
+        {"join-small": run_small_join, "join-skew": run_skew_join, "join-batch": run_batch_join, "serve": run_serve, "hash": run_hash_bench}[args.workload](args)
         return
     if args.small:
         args.shift = max(args.shift, 3)
