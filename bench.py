@@ -683,6 +683,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="time the planner's own plan, without the autotuner")
     ap.add_argument("--workload", default="join", choices=["join", "join-small", "join-skew", "join-batch", "serve", "hash"], help="join: the 2^27 x 2^29 int64 join (default); the others print their own line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -729,6 +730,10 @@ def main():
     t_r = vj.table(rk, rp, nr, 2, 8)
     t_s = vj.table(sk, sp, ns, 2, 8)
     stream = torch.cuda.current_stream()
+
+    # the autotuner picks the plan (radix split, table size, table kind) for this shape
+    # class before the timed region; the timed joins are automatic and use it
+    tuned_opts, tuned_ms = (None, None) if args.no_tune else ctx.tune(t_r, t_s, out, cap, stream=stream)
 
     def step():
         return ctx.join(t_r, t_s, None, out=out, capacity=cap, stream=stream)
@@ -836,6 +841,10 @@ def main():
     cfg["radix_bits"] = prof0["radix_bits"][:passes]
     cfg["build_rows_per_table"] = prof0["build_rows"]
     cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
+    cfg["tables"] = prof0.get("tables")
+    if tuned_opts is not None:
+        cfg["tuned_plan"] = vj.options_dict(tuned_opts)
+        cfg["tuner_best_ms"] = tuned_ms
     lat = sorted(step_ms)
 
     def pct(q):

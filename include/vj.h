@@ -259,6 +259,24 @@ VJ_API int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const
 VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
 
 /*
+ * Autotuner. The reference sweeps its tunables (bucket counts, vector sizes, kernel shapes)
+ * from TOML grids in separate benchmark runs (src/benchmark/configuration.hpp:200-305).
+ * vj_tune runs candidate plans of a join of r and s on this context -- the planner's
+ * choice, two passes with the bits split both ways around the total that fills the
+ * shared-memory tables (and one bit more or less), one pass, L2-resident tables for large
+ * build sides; at most max_candidates (0 = 12) -- each a full join into d_pairs (capacity
+ * pairs), and keeps the fastest for the join's shape class (key words, payload bytes,
+ * ceil(log2 |R|), ceil(log2 |S|), hash algorithm and width of `base`). Later vj_join calls
+ * on this context with automatic options (NULL or all fields zero but the hash) of that
+ * class use it. *best / *best_ms (optional) receive the winner and its time.
+ * vj_tune_save / vj_tune_load write / merge the context's cache as a text file.
+ */
+VJ_API int vj_tune(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *base, void *d_pairs, uint64_t capacity, int max_candidates, vj_join_options *best, float *best_ms,
+                   vj_stream_t stream);
+VJ_API int vj_tune_save(const vj_ctx *ctx, const char *path);
+VJ_API int vj_tune_load(vj_ctx *ctx, const char *path);
+
+/*
  * vj_join_batch -- many independent joins in one launch sequence. The reference runs one
  * JoinProvider::join per call; its nearest counterpart is the bucket-pair work list of a
  * single join (src/join/join_provider.cuh:717-795).

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdarg>
+#include <vector>
 
 #include "vj.h"
 
@@ -384,6 +385,17 @@ struct DeviceInfo {
 
 int device_info(int device, DeviceInfo *out);
 
+// Tuning cache: the fastest plan found for a class of join shapes.
+struct TuneKey {
+    int32_t kw, pb, lg_r, lg_s, algo, hash_bits;
+    bool operator==(const TuneKey &o) const { return kw == o.kw && pb == o.pb && lg_r == o.lg_r && lg_s == o.lg_s && algo == o.algo && hash_bits == o.hash_bits; }
+};
+struct TuneEntry {
+    TuneKey key;
+    vj_join_options opt;
+    float ms;
+};
+
 }  // namespace vj
 
 // Context (defined in vj_runtime.cu).
@@ -401,6 +413,7 @@ struct vj_ctx {
     bool events_ready;
     vj_profile last;         // filled after each join when profiling
     int launches;            // library kernels launched by the current join
+    std::vector<vj::TuneEntry> tuned;  // vj_tune results, consulted by automatic joins
 };
 
 namespace vj {
@@ -419,6 +432,9 @@ void profile_mark(vj_ctx *ctx, int mark, cudaStream_t stream);
 int workspace_reserve(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
 int owned_alloc(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
 void owned_release(vj_ctx *ctx, size_t bytes);
+// Shape class of a join (vj_tune's cache key) and the tuned options for an automatic join.
+TuneKey tune_key(const vj_table *r, const vj_table *s, const vj_join_options *opt);
+const vj_join_options *tuned_options(const vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *opt);
 // Upper estimate of the device bytes a vj_join of r and s takes from a context.
 int join_footprint(const vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *opt, uint64_t *bytes);
 }  // namespace vj

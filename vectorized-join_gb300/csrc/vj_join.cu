@@ -1031,6 +1031,7 @@ extern "C" int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const 
     if (r->rows == 0 || s->rows == 0) {
         return VJ_OK;  // empty join: count 0, no buffer needed
     }
+    call.opt = tuned_options(ctx, r, s, options);  // a vj_tune result for this shape class, if any
     return dispatch(r->key_words, r->payload_bytes, 0, call);
 }
 

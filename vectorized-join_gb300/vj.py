@@ -59,6 +59,9 @@ EXPORTS = [
     "vj_build_probe",
     "vj_join",
     "vj_join_batch",
+    "vj_tune",
+    "vj_tune_save",
+    "vj_tune_load",
     "vj_server_create",
     "vj_server_submit",
     "vj_server_wait",
@@ -95,6 +98,17 @@ class VjJoinOptions(ctypes.Structure):
         ("probe_sub_rows", ctypes.c_int32),
         ("reserved", ctypes.c_int32 * 4),
     ]
+
+
+def options_dict(o: "VjJoinOptions") -> dict:
+    return {
+        "tables": "l2" if o.flags & VJ_JOIN_L2_TABLES else ("shared" if o.flags & VJ_JOIN_SHARED_TABLES else "auto"),
+        "passes": o.passes if o.flags & VJ_JOIN_FIXED_PASSES else "auto",
+        "radix_bits": [o.radix_bits[0], o.radix_bits[1]],
+        "build_rows": o.build_rows,
+        "probe_threads": o.probe_threads,
+        "probe_sub_rows": o.probe_sub_rows,
+    }
 
 
 class VjResult(ctypes.Structure):
@@ -228,6 +242,12 @@ def load() -> ctypes.CDLL:
         L.vj_server_stats_get.argtypes = [vp, ctypes.POINTER(VjServerStats)]
         L.vj_server_destroy.restype = i32
         L.vj_server_destroy.argtypes = [vp]
+        L.vj_tune.restype = i32
+        L.vj_tune.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), vp, u64, i32, ctypes.POINTER(VjJoinOptions), ctypes.POINTER(ctypes.c_float), vp]
+        L.vj_tune_save.restype = i32
+        L.vj_tune_save.argtypes = [vp, ctypes.c_char_p]
+        L.vj_tune_load.restype = i32
+        L.vj_tune_load.argtypes = [vp, ctypes.c_char_p]
         L.vj_join_host.restype = i32
         L.vj_join_host.argtypes = [vp, ctypes.POINTER(VjTable), ctypes.POINTER(VjTable), ctypes.POINTER(VjJoinOptions), vp, u64, ctypes.POINTER(u64), vp]
         L.vj_result_free.restype = i32
@@ -374,6 +394,19 @@ class Context:
                 ptr(counts), ptr(status), stream_handle(stream)
             )
         )
+
+    def tune(self, r: VjTable, s: VjTable, out, capacity: int, base: VjJoinOptions | None = None, max_candidates: int = 0, stream=None) -> tuple[VjJoinOptions, float]:
+        """vj_tune: the fastest plan for this join's shape class (kept in the context)."""
+        best = VjJoinOptions()
+        ms = ctypes.c_float(0)
+        check(self.lib.vj_tune(self.handle, ctypes.byref(r), ctypes.byref(s), ctypes.byref(base) if base else None, ptr(out), capacity, max_candidates, ctypes.byref(best), ctypes.byref(ms), stream_handle(stream)))
+        return best, float(ms.value)
+
+    def tune_save(self, path: str) -> None:
+        check(self.lib.vj_tune_save(self.handle, str(path).encode()))
+
+    def tune_load(self, path: str) -> None:
+        check(self.lib.vj_tune_load(self.handle, str(path).encode()))
 
     def join_host(self, r: VjTable, s: VjTable, out, capacity: int, opts: VjJoinOptions | None = None, stream=None) -> int:
         n = u64(0)
