@@ -315,6 +315,7 @@ struct JoinRun {
     int threads;       // probe block size
     size_t probe_smem;
     int probe_grid;
+    unsigned long long *plan_blocks = nullptr;  // per-block item offsets of the item planner
     // batches of joins: per-join item counts, partitions per join
     bool batch = false;
     uint32_t *batch_cnt = nullptr;
@@ -370,6 +371,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
                               : batch                     ? 2ull * ((uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap) + 4096
                                                           : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
     uint32_t *b_seg_begin = nullptr, *b_seg_end = nullptr, *b_cnt = nullptr;
+    unsigned long long *plan_blocks = nullptr;
     unsigned long long *b_out_begin = nullptr;
     const bool l2 = pl.tables == VJ_TABLES_L2;
     const uint32_t max_seqs = l2 ? (uint32_t)(np + in.rows[0] / pl.l2_rc + 1) : 0;
@@ -401,6 +403,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         if (pl.passes >= 1) *pb0 = carve_pass(c, G0, bins0, max_units[0]);
         if (pl.passes >= 2) *pb1 = carve_pass(c, G1, bins1, max_units[1]);
         *item_begin = c.take<uint32_t>((size_t)np + 2);
+        plan_blocks = c.take<unsigned long long>(((size_t)np + PLAN_BLOCK - 1) / PLAN_BLOCK);
         *item_desc = c.take<uint4>(item_cap);
         *ticket = c.take<uint32_t>(1);
         *out_count = c.take<unsigned long long>(1);
@@ -513,6 +516,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         run->batch_parts = (uint32_t)(np / J);
     }
     run->probe = Pq;
+    run->plan_blocks = plan_blocks;
     run->d_out_count = out_count;
     run->d_error = error;
     if (l2) {
@@ -574,8 +578,14 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         VJ_CUDA(cudaGetLastError());
         ctx->launches += 2;
     } else {
-        plan_items_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe);
+        const int nb = (run.probe.np + PLAN_BLOCK - 1) / PLAN_BLOCK;
+        items_count_kernel<<<nb, PLAN_BLOCK, 0, stream>>>(run.probe, run.plan_blocks);
         VJ_CUDA(cudaGetLastError());
+        items_scan_kernel<<<1, PLAN_THREADS, 0, stream>>>(run.probe, run.plan_blocks, nb);
+        VJ_CUDA(cudaGetLastError());
+        items_write_kernel<<<nb, PLAN_BLOCK, 0, stream>>>(run.probe, run.plan_blocks);
+        VJ_CUDA(cudaGetLastError());
+        ctx->launches += 2;
     }
     if (run.aos) {
         if (run.batch) probe_kernel<KW, PB, HS, true, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);

@@ -657,40 +657,59 @@ __device__ __forceinline__ unsigned long long items_of(const ProbeParams &Q, int
     return (unsigned long long)((nr + Q.rcap - 1) / Q.rcap) * ((ns + Q.schunk - 1) / Q.schunk);
 }
 
-// One block. Work items per partition, their prefix and the partition of every item;
-// resets the ticket and counter. A plan of 2^31 or more items (only reachable when almost
-// every row shares one hash) is refused with error flag 2 and no items.
-__global__ void __launch_bounds__(PLAN_THREADS) plan_items_kernel(ProbeParams Q) {
+// Work items, in three launches over blocks of PLAN_BLOCK partitions: items per partition
+// and their prefix inside the block; the blocks' offsets and the total (the ticket and the
+// counter reset); the global prefix and the item descriptors. A plan of 2^31 or more items
+// (only reachable when almost every row shares one hash) is refused with error flag 2 and
+// no items.
+constexpr int PLAN_BLOCK = 256;
+
+__global__ void __launch_bounds__(PLAN_BLOCK) items_count_kernel(ProbeParams Q, unsigned long long *block_tot) {
     __shared__ unsigned long long s_warp[32];
-    const int per = (Q.np + PLAN_THREADS - 1) / PLAN_THREADS;
-    const int p0 = threadIdx.x * per;
+    const int p = blockIdx.x * PLAN_BLOCK + threadIdx.x;
+    const unsigned long long n = p < Q.np ? items_of(Q, p) : 0ull;
+    unsigned long long tot = 0;
+    const unsigned long long ex = block_exclusive_scan<unsigned long long>(n, s_warp, &tot);
+    if (p < Q.np) Q.item_begin[p] = (uint32_t)(ex < 0xffffffffull ? ex : 0xffffffffull);
+    if (threadIdx.x == 0) block_tot[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(PLAN_THREADS) items_scan_kernel(ProbeParams Q, unsigned long long *block_tot, int nblocks) {
+    __shared__ unsigned long long s_warp[32];
+    const int per = (nblocks + PLAN_THREADS - 1) / PLAN_THREADS;
+    const int b0 = threadIdx.x * per;
     unsigned long long mine = 0;
-    for (int p = p0; p < p0 + per && p < Q.np; p++) mine += items_of(Q, p);
+    for (int b = b0; b < b0 + per && b < nblocks; b++) mine += block_tot[b];
     unsigned long long total = 0;
     unsigned long long run = block_exclusive_scan<unsigned long long>(mine, s_warp, &total);
-    const bool too_many = total >= (1ull << 31);
-    const bool fill = !too_many && total <= Q.item_cap;
-    for (int p = p0; p < p0 + per && p < Q.np; p++) {
-        Q.item_begin[p] = too_many ? 0u : (uint32_t)run;
-        const unsigned long long n = items_of(Q, p);
-        if (fill && n) {
-            const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
-            const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
-            for (uint32_t r0 = rb; r0 < re; r0 += Q.rcap) {
-                for (uint32_t s0 = sb; s0 < se; s0 += Q.schunk) {
-                    Q.item_desc[run++] = make_uint4(r0, min(re, r0 + Q.rcap), s0, min(se, s0 + Q.schunk));
-                }
-            }
-        } else {
-            run += n;
-        }
+    for (int b = b0; b < b0 + per && b < nblocks; b++) {
+        const unsigned long long t = block_tot[b];
+        block_tot[b] = run;
+        run += t;
     }
     if (threadIdx.x == 0) {
+        const bool too_many = total >= (1ull << 31);
+        const bool fill = !too_many && total <= Q.item_cap;
         Q.item_begin[Q.np] = too_many ? 0u : (uint32_t)total;
         Q.item_begin[Q.np + 1] = fill ? 1u : 0u;
         if (too_many) atomicOr(Q.error, 2u);
         *Q.ticket = 0;
         *Q.out_count = 0;
+    }
+}
+
+__global__ void __launch_bounds__(PLAN_BLOCK) items_write_kernel(ProbeParams Q, const unsigned long long *block_base) {
+    const int p = blockIdx.x * PLAN_BLOCK + threadIdx.x;
+    if (p >= Q.np) return;
+    unsigned long long run = block_base[blockIdx.x] + Q.item_begin[p];
+    Q.item_begin[p] = (uint32_t)(run < 0xffffffffull ? run : 0xffffffffull);
+    if (Q.item_begin[Q.np + 1] == 0u || !items_of(Q, p)) return;  // descriptors only when they all fit
+    const uint32_t rb = Q.r_begin ? Q.r_begin[p] : 0, re = Q.r_begin ? Q.r_end[p] : Q.r_rows;
+    const uint32_t sb = Q.s_begin ? Q.s_begin[p] : 0, se = Q.s_begin ? Q.s_end[p] : Q.s_rows;
+    for (uint32_t r0 = rb; r0 < re; r0 += Q.rcap) {
+        for (uint32_t s0 = sb; s0 < se; s0 += Q.schunk) {
+            Q.item_desc[run++] = make_uint4(r0, min(re, r0 + Q.rcap), s0, min(se, s0 + Q.schunk));
+        }
     }
 }
 
@@ -952,20 +971,23 @@ __global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
             s_rows = s_next_rows;
             s_join = s_next_join;
             s_dups = 0;
-            if (s_item < total_items) {
-                s_next_item = atomicAdd(Q.ticket, 1u);
-                if (s_next_item < total_items) {
-                    const uint4 d = item_rows(Q, s_next_item, direct);
-                    s_next_rows = d;
-                    if constexpr (BATCH) s_next_join = join_of(Q, d.z);
-                    C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
-                    C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
-                }
-            }
         }
         __syncthreads();
         const uint32_t item = s_item;
         if (item >= total_items) break;
+        if (threadIdx.x == 32) {
+            // claim the next item and start its rows towards L2; its latency overlaps this
+            // item's build-chunk copy (thread 0 drives the copies)
+            const uint32_t nx = atomicAdd(Q.ticket, 1u);
+            s_next_item = nx;
+            if (nx < total_items) {
+                const uint4 dn = item_rows(Q, nx, direct);
+                s_next_rows = dn;
+                if constexpr (BATCH) s_next_join = join_of(Q, dn.z);
+                C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, dn.x, dn.y);
+                C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, dn.z, dn.w);
+            }
+        }
         const uint4 d = s_rows;
         const uint32_t r0 = d.x, r1 = d.y, s0 = d.z, s1 = d.w;
         const uint32_t join = BATCH ? s_join : 0u;
