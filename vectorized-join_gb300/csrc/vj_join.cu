@@ -372,6 +372,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
                                                           : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
     uint32_t *b_seg_begin = nullptr, *b_seg_end = nullptr, *b_cnt = nullptr;
     unsigned long long *plan_blocks = nullptr;
+    uint16_t *bids[2] = {nullptr, nullptr};  // pass-2 buckets written by pass 1
     unsigned long long *b_out_begin = nullptr;
     const bool l2 = pl.tables == VJ_TABLES_L2;
     const uint32_t max_seqs = l2 ? (uint32_t)(np + in.rows[0] / pl.l2_rc + 1) : 0;
@@ -394,6 +395,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
                 bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
             }
         }
+        for (int sd = 0; sd < 2; sd++) bids[sd] = pl.passes >= 2 ? c.take<uint16_t>((size_t)in.rows[sd] + 8) : nullptr;
         if (batch) {
             b_seg_begin = c.take<uint32_t>((size_t)2 * J);
             b_seg_end = c.take<uint32_t>((size_t)2 * J);
@@ -447,7 +449,11 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
             P.side[sd].rows_in = pass > 0 ? bufs[pass - 1][sd] : nullptr;
             P.side[sd].rows_out = bufs[pass][sd];
             P.side[sd].rows = in.rows[sd];
+            P.side[sd].bid_out = pass == 0 && pl.passes >= 2 ? bids[sd] : nullptr;
+            P.side[sd].bid_in = pass == 1 ? bids[sd] : nullptr;
         }
+        P.next_shift = 64 - (pl.bits[0] + pl.bits[1]);
+        P.next_bits = pl.bits[1];
         P.nsides = 2;
         P.Q = Q;
         P.seg_begin = seg_begin;

@@ -64,6 +64,10 @@ struct Side {
     void *pay_out;
     void *hash_out;        // HS != 0 only (may be null: hashes not moved)
     uint32_t rows;
+    // the next pass's bucket of every output row (u16 at the row's output position), written
+    // by a first pass whose second pass then counts these instead of re-reading the rows
+    uint16_t *bid_out;
+    const uint16_t *bid_in;
 };
 
 struct PassParams {
@@ -86,6 +90,7 @@ struct PassParams {
     uint32_t *part_begin;        // [G*bins]
     uint32_t *part_end;          // [G*bins]
     uint32_t *error;             // bit 4: a bulk-copy wait ran out
+    int next_shift, next_bits;   // bucket of the next pass (bid_out)
 };
 
 struct ProbeParams {
@@ -428,6 +433,26 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
     const uint64_t mask = bins - 1;
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
     __syncthreads();
+    if (S.bid_in) {
+        // buckets written by the previous pass: 2 bytes a row instead of the row
+        constexpr int UB = 8;
+        uint32_t i = U.y + threadIdx.x;
+        for (; i + (UB - 1) * PART_THREADS < U.z; i += UB * PART_THREADS) {
+            uint32_t v[UB];
+#pragma unroll
+            for (int k = 0; k < UB; k++) v[k] = __ldcs(S.bid_in + i + k * PART_THREADS);
+#pragma unroll
+            for (int k = 0; k < UB; k++) atomicAdd(&s_hist[v[k] & mask], 1u);
+        }
+        for (; i < U.z; i += PART_THREADS) atomicAdd(&s_hist[__ldcs(S.bid_in + i) & mask], 1u);
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
+            uint32_t c = s_hist[b];
+            P.cnt[(size_t)u * bins + b] = c;
+            if (c) atomicAdd(&P.seg_tot[(size_t)U.x * bins + b], c);
+        }
+        return;
+    }
     constexpr int UNROLL = 4;
     constexpr uint32_t STEP = UNROLL * PART_THREADS;
     // keep the next AHEAD steps of this unit on their way to L2
@@ -505,18 +530,18 @@ struct ScatterSmem {
     using L = Layout<KW, PB, HS>;
     static constexpr int T = PART_THREADS * ITEMS;
     static constexpr size_t IN_BUF = Chunk<KW, PB, HS, IN_AOS>::bytes(T);
-    static constexpr size_t OUT = (size_t)T * (L::STRIDE + 2);
+    static constexpr size_t OUT = (size_t)T * (L::STRIDE + 4);  // rows + bucket word per row
     static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 3 * 4; }
 };
 
-// Rows per thread of a scatter tile: the largest of 4, 2, 1 whose block (with 2^10 bins)
+// Rows per thread of a scatter tile: the largest of 4, 2, 1 whose block (with 2^9 bins)
 // stays within about half of an SM's shared memory, so two blocks fit per SM (wider
 // passes, up to 2^12 bins, stay below the 227 KB block limit with one block per SM).
 template <int KW, int PB, int HS, bool IN_AOS>
 constexpr int scatter_items() {
-    return ScatterSmem<KW, PB, HS, IN_AOS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 4>::OUT + 16 + 1024 * 12 <= 113 * 1024   ? 4
-           : ScatterSmem<KW, PB, HS, IN_AOS, 2>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 2>::OUT + 16 + 1024 * 12 <= 113 * 1024 ? 2
-                                                                                                                                     : 1;
+    return ScatterSmem<KW, PB, HS, IN_AOS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 4>::OUT + 16 + 512 * 12 <= 113 * 1024   ? 4
+           : ScatterSmem<KW, PB, HS, IN_AOS, 2>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 2>::OUT + 16 + 512 * 12 <= 113 * 1024 ? 2
+                                                                                                                                   : 1;
 }
 
 template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS>
@@ -530,7 +555,8 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     uint64_t *bar = (uint64_t *)s_raw;
     unsigned char *inb0 = s_raw + 16;
     unsigned char *out_rows = inb0 + 2 * SM::IN_BUF;
-    uint16_t *st_b = (uint16_t *)(out_rows + (size_t)T * L::STRIDE);
+    // bucket of each staged row, and in the high half the next pass's bucket (bid_out)
+    uint32_t *st_b = (uint32_t *)(out_rows + (size_t)T * L::STRIDE);
     const uint32_t bins = 1u << P.bits;
     uint32_t *s_run = (uint32_t *)(st_b + T);
     uint32_t *s_cnt = s_run + bins;
@@ -585,11 +611,16 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         const C in = C::view(inb0 + buf * SM::IN_BUF, T, s_delta[buf]);
         uint32_t bk[ITEMS];
         uint32_t rk[ITEMS];
+        uint32_t nb[ITEMS];
+        const uint64_t nmask = (1ull << P.next_bits) - 1;
 #pragma unroll
         for (int j = 0; j < ITEMS; j++) {
             const uint32_t i = j * PART_THREADS + threadIdx.x;
+            nb[j] = 0;
             if (i < nt) {
-                bk[j] = (uint32_t)((bucket_hash(in.h_of(i, P.hs), P.hs) >> P.shift) & mask);
+                const uint64_t mh = bucket_hash(in.h_of(i, P.hs), P.hs);
+                bk[j] = (uint32_t)((mh >> P.shift) & mask);
+                if (OUT_AOS) nb[j] = (uint32_t)((mh >> P.next_shift) & nmask);
                 rk[j] = atomicAdd(&s_cnt[bk[j]], 1u);
             }
         }
@@ -610,7 +641,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
             if (i < nt) {
                 const uint32_t pos = s_start[bk[j]] + rk[j];
                 in.copy_row(i, out_rows + (size_t)pos * L::STRIDE);
-                st_b[pos] = (uint16_t)bk[j];
+                st_b[pos] = bk[j] | (nb[j] << 16);
             }
         }
         __syncthreads();  // input buffer `buf` is free: refill it with tile k + 2
@@ -620,10 +651,12 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
             C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T), T, inb0 + buf * SM::IN_BUF, &bar[buf], s_delta[buf]);
         }
         for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
-            const uint32_t b = st_b[i];
+            const uint32_t sbk = st_b[i];
+            const uint32_t b = sbk & 0xffffu;
             const uint32_t dst = s_run[b] + i - s_start[b];
             const unsigned char *row = out_rows + (size_t)i * L::STRIDE;
             if (OUT_AOS) {
+                if (S.bid_out) S.bid_out[dst] = (uint16_t)(sbk >> 16);
                 unsigned char *g = (unsigned char *)S.rows_out + (size_t)dst * L::STRIDE;
                 if (L::STRIDE % 16 == 0) {
 #pragma unroll
