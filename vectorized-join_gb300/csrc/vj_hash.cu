@@ -94,15 +94,18 @@ __global__ void __launch_bounds__(HASH_THREADS) hash_kernel(const uint8_t *__res
     const uint64_t stride = (uint64_t)gridDim.x * HASH_THREADS;
     uint64_t e = (uint64_t)blockIdx.x * HASH_THREADS + threadIdx.x;
     if constexpr (EB > 0) {
-        // HASH_UNROLL independent elements per thread per step keep several loads in flight.
-        for (; e + (HASH_UNROLL - 1) * stride < n; e += HASH_UNROLL * stride) {
-            uint32_t w[HASH_UNROLL][EB / 4];
+        // UN independent elements per thread per step keep several loads in flight; 32-byte
+        // elements run one per thread over a grid that covers them all (faster on GB300:
+        // new blocks keep every SM full where grid-stride threads would serialise).
+        constexpr int UN = EB == 32 ? 1 : HASH_UNROLL;
+        for (; e + (UN - 1) * stride < n; e += UN * stride) {
+            uint32_t w[UN][EB / 4];
 #pragma unroll
-            for (int u = 0; u < HASH_UNROLL; u++) {
+            for (int u = 0; u < UN; u++) {
                 load_element<EB>(in, e + u * stride, w[u]);
             }
 #pragma unroll
-            for (int u = 0; u < HASH_UNROLL; u++) {
+            for (int u = 0; u < UN; u++) {
                 __stcs(out + e + u * stride, hash_words<H, CB, ALGO, EB / 4>(w[u], chunk_offset));
             }
         }
@@ -206,10 +209,12 @@ extern "C" int vj_hash(const void *d_elements, uint64_t n, int chunk_offset, int
     VJ_CUDA(cudaGetDevice(&device));
     DeviceInfo info;
     VJ_TRY(device_info(device, &info));
-    // Grid: 8 resident blocks of 256 threads per SM, or fewer for small inputs.
-    const uint64_t per_block = (uint64_t)HASH_THREADS * HASH_UNROLL;
+    // Grid: 8 resident blocks of 256 threads per SM, or fewer for small inputs; 32-byte
+    // elements (one per thread) get a block per 256 elements.
+    const bool wide = chunk_bits >= 32 && element_chunks * (chunk_bits / 8) == 32 && chunk_offset == 0;
+    const uint64_t per_block = (uint64_t)HASH_THREADS * (wide ? 1 : HASH_UNROLL);
     uint64_t blocks = (n + per_block - 1) / per_block;
-    const uint64_t max_blocks = (uint64_t)info.sms * 8;
+    const uint64_t max_blocks = wide ? (1ull << 31) - 1 : (uint64_t)info.sms * 8;
     int grid = (int)(blocks < max_blocks ? (blocks ? blocks : 1) : max_blocks);
     const uint8_t *in = (const uint8_t *)d_elements;
     cudaStream_t s = (cudaStream_t)stream;
