@@ -171,8 +171,10 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     }
     const int G0 = 2;
     const int G1 = 2 << pl.bits[0];
-    pl.max_units[0] = info.sms * 16 + G0;
-    pl.max_units[1] = info.sms * 16 + G1;
+    // 64 work units per SM: short units keep the SMs full as blocks finish (16 per SM was
+    // 0.26 ms slower on the 2^27 x 2^29 join, 256 per SM slower still in the scatters)
+    pl.max_units[0] = info.sms * 64 + G0;
+    pl.max_units[1] = info.sms * 64 + G1;
     return pl;
 }
 
@@ -362,8 +364,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     const int np = J * (pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1));
     int max_units[2] = {pl.max_units[0], pl.max_units[1]};
     if (batch) {
-        max_units[0] = ctx->info.sms * 16 + G0;
-        max_units[1] = ctx->info.sms * 16 + G1;
+        max_units[0] = ctx->info.sms * 64 + G0;
+        max_units[1] = ctx->info.sms * 64 + G1;
     }
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
