@@ -10,7 +10,9 @@
 #include "vj_l2_kernels.cuh"
 
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 namespace vj {
 
@@ -180,13 +182,40 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
 
 // ------------------------------------------------------------------ kernel attributes
 
+// Per (kernel, device): the dynamic shared memory already allowed, and occupancies already
+// asked for -- driver calls a join would otherwise repeat on every call.
+std::mutex g_attr_mutex;
+std::map<std::pair<const void *, int>, size_t> g_smem_allowed;
+std::map<std::tuple<const void *, int, int, size_t>, int> g_occupancy;
+
 template <typename K>
 int ensure_smem(K kernel, size_t bytes) {
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lock(mu);
-    if (bytes > 48 * 1024) {
-        VJ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    if (bytes <= 48 * 1024) return VJ_OK;
+    int dev = 0;
+    VJ_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    size_t &allowed = g_smem_allowed[std::make_pair((const void *)kernel, dev)];
+    if (allowed >= bytes) return VJ_OK;
+    VJ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    allowed = bytes;
+    return VJ_OK;
+}
+
+template <typename K>
+int blocks_per_sm(K kernel, int threads, size_t smem, int *per_sm) {
+    int dev = 0;
+    VJ_CUDA(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> lock(g_attr_mutex);
+        auto it = g_occupancy.find(std::make_tuple((const void *)kernel, dev, threads, smem));
+        if (it != g_occupancy.end()) {
+            *per_sm = it->second;
+            return VJ_OK;
+        }
     }
+    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kernel, threads, smem));
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    g_occupancy[std::make_tuple((const void *)kernel, dev, threads, smem)] = *per_sm;
     return VJ_OK;
 }
 
@@ -248,7 +277,7 @@ int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
 int probe_grid(const DeviceInfo &info, int threads, size_t smem, int *grid) {
     int per_sm = 0;
-    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe_kernel<KW, PB, HS, AOS, BATCH>, threads, smem));
+    VJ_TRY(blocks_per_sm(probe_kernel<KW, PB, HS, AOS, BATCH>, threads, smem, &per_sm));
     if (per_sm < 1) per_sm = 1;
     *grid = info.sms * per_sm;
     return VJ_OK;
@@ -335,7 +364,7 @@ int l2_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     run->l2_smem = (size_t)L2_WARPS * L2_WARP_STAGE * 2 * PB;
     VJ_TRY(ensure_smem(l2_join_kernel<KW, PB, HS>, run->l2_smem));
     int per_sm = 0;
-    VJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, l2_join_kernel<KW, PB, HS>, L2_THREADS, run->l2_smem));
+    VJ_TRY(blocks_per_sm(l2_join_kernel<KW, PB, HS>, L2_THREADS, run->l2_smem, &per_sm));
     VJ_CHECK(per_sm >= 1, VJ_ERR_UNSUPPORTED, "L2-table probe kernel does not fit an SM");
     run->l2_grid = per_sm * ctx->info.sms;  // all resident: the cooperative launch checks it
     return VJ_OK;
