@@ -251,8 +251,13 @@ VJ_API int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_j
 /*
  * vj_join_host -- the same join with HOST tables and a HOST output buffer: copies r and s
  * to the device, joins, and copies the pairs back (up to capacity pairs). Host memory that
- * is page-locked transfers at full link speed. Returns VJ_ERR_CAPACITY with *count = needed
- * when capacity is too small (nothing is copied back then).
+ * is page-locked transfers at full link speed. A probe side of at least twice the build
+ * side and 2^23 rows is pipelined: it is copied in chunks of about |R| rows (2 to 16), each
+ * chunk is joined with the whole build side as soon as it has landed, and its pairs are
+ * copied back while the next chunk is joined (copies in, joins and copies out overlap; the
+ * pairs are the same, grouped by chunk). Returns when the pairs are in h_pairs. Returns
+ * VJ_ERR_CAPACITY with *count = needed when capacity is too small; h_pairs then holds an
+ * unspecified part of the pairs. With profiling on, the profile is that of the last chunk.
  */
 VJ_API int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, vj_stream_t stream);
 

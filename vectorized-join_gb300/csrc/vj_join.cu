@@ -927,7 +927,7 @@ struct BuildProbeCall {
         Plan pl;
         JoinRun run;
         uint64_t n = 0;
-        VJ_TRY((probe_once<KW, PB, HS>(c.ctx, c.t, c.hs, nullptr, -1, rr.pairs, rr.capacity, c.stream, &run, &pl, &n)));
+        VJ_TRY((probe_once<KW, PB, HS>(c.ctx, c.t, c.hs, c.opt, -1, rr.pairs, rr.capacity, c.stream, &run, &pl, &n)));
         finish_profile(c.ctx, pl, c.t.rows[0], c.t.rows[1], n);
         rr.count = n;
         return VJ_OK;
@@ -1158,6 +1158,215 @@ extern "C" int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashe
     return dispatch(in->key_words, in->payload_bytes, d_hashes_in ? hash_bits / 8 : 0, call);
 }
 
+// Copies n words from page-locked, mapped host memory to the device with SM loads, eight
+// in flight per thread. The copy engine's reads of host memory stall now and then on this
+// platform (1 GB taking 40-50 ms instead of 5 at times, with or without other GPU work),
+// while loads from a few SMs, which keep many host pages in flight at once, hold the link
+// rate of ~210 GB/s throughout.
+template <typename V>
+__global__ void __launch_bounds__(512) host_copy_kernel(const V *__restrict__ src, V *__restrict__ dst, size_t n) {
+    constexpr int U = 8;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < n; i += U * stride) {
+        V v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) v[u] = src[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < U; u++) dst[i + u * stride] = v[u];
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+namespace {
+
+// Blocks of host_copy_kernel: 16 x 512 threads x 8 loads of 16 bytes keep 1 MB in flight,
+// enough for the link, and leave the other SMs to the joins they overlap.
+constexpr int HOST_COPY_BLOCKS = 16;
+
+// Device address of host memory [p, p + bytes) that the GPU can load from (page-locked and
+// mapped, both ends in the same mapping), or null.
+const char *mapped_host(const void *p, size_t bytes) {
+    if (!p || bytes == 0) return nullptr;
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    if (cudaPointerGetAttributes(&b, (const char *)p + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (b.type != cudaMemoryTypeHost || (const char *)b.devicePointer != (const char *)a.devicePointer + bytes - 1) return nullptr;
+    return (const char *)a.devicePointer;
+}
+
+// Host-to-device copy: SM loads for mapped page-locked memory, the copy engine otherwise
+// (pageable memory, which it stages itself).
+cudaError_t copy_in(void *dst, const void *src, size_t bytes, cudaStream_t stream) {
+    if (bytes == 0) return cudaSuccess;
+    const char *dsrc = mapped_host(src, bytes);
+    if (!dsrc) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+    const uintptr_t al = (uintptr_t)dsrc | (uintptr_t)dst | (uintptr_t)bytes;
+    const dim3 grid(HOST_COPY_BLOCKS), block(512);
+    if ((al & 15) == 0) {
+        host_copy_kernel<uint4><<<grid, block, 0, stream>>>((const uint4 *)dsrc, (uint4 *)dst, bytes / 16);
+    } else if ((al & 7) == 0) {
+        host_copy_kernel<uint2><<<grid, block, 0, stream>>>((const uint2 *)dsrc, (uint2 *)dst, bytes / 8);
+    } else if ((al & 3) == 0) {
+        host_copy_kernel<uint32_t><<<grid, block, 0, stream>>>((const uint32_t *)dsrc, (uint32_t *)dst, bytes / 4);
+    } else {
+        host_copy_kernel<uint8_t><<<grid, block, 0, stream>>>((const uint8_t *)dsrc, (uint8_t *)dst, bytes);
+    }
+    return cudaGetLastError();
+}
+
+// A join into a caller's device buffer that is never reallocated, capacity 0 included
+// (counts only: the kernels write nothing at or past the capacity).
+int join_into(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *d_pairs, uint64_t capacity, uint64_t *count, cudaStream_t stream) {
+    *count = 0;
+    if (r->rows == 0 || s->rows == 0) return VJ_OK;
+    vj_result res{};
+    res.pairs = d_pairs;
+    res.capacity = capacity;
+    res.owned = 0;
+    JoinCall call;
+    call.ctx = ctx;
+    call.t.keys[0] = r->keys;
+    call.t.keys[1] = s->keys;
+    call.t.pay[0] = r->payloads;
+    call.t.pay[1] = s->payloads;
+    call.t.hash[0] = call.t.hash[1] = nullptr;
+    call.t.rows[0] = (uint32_t)r->rows;
+    call.t.rows[1] = (uint32_t)s->rows;
+    call.hs = spec_from(options, 1);
+    call.opt = tuned_options(ctx, r, s, options);
+    call.res = &res;
+    call.stream = stream;
+    BuildProbeCall cc{call};
+    VJ_TRY(dispatch(r->key_words, r->payload_bytes, 0, cc));
+    *count = res.count;
+    return VJ_OK;
+}
+
+// Probe-side chunks of vj_join_host's pipeline. A chunk's join (the whole build side and
+// the chunk) takes about as long as the copy of one build side's worth of probe rows, so
+// chunks of about |R| rows keep the link busy; 1 (no pipeline) for a probe side under
+// twice the build side or a join too small to gain from it.
+int host_chunks(uint64_t r_rows, uint64_t s_rows) {
+    const uint64_t min_chunk = 1ull << 22;
+    if (r_rows == 0 || s_rows < 2 * r_rows || s_rows < 2 * min_chunk) return 1;
+    uint64_t c = (s_rows + r_rows / 2) / r_rows;
+    if (s_rows / c < min_chunk) c = s_rows / min_chunk;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(c, 16));
+}
+
+int host_streams(vj_ctx *ctx) {
+    if (ctx->host_ready) return VJ_OK;
+    cudaStream_t in = nullptr, out = nullptr;
+    cudaEvent_t ev[sizeof(ctx->host_ev) / sizeof(ctx->host_ev[0])] = {};
+    const int n = (int)(sizeof(ev) / sizeof(ev[0]));
+    // copies in at the highest priority: their blocks are scheduled ahead of the joins'
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&in, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&out, cudaStreamNonBlocking);
+    for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        for (int i = 0; i < n; i++)
+            if (ev[i]) cudaEventDestroy(ev[i]);
+        if (in) cudaStreamDestroy(in);
+        if (out) cudaStreamDestroy(out);
+        return cuda_error(e, "vj_join_host: copy streams");
+    }
+    ctx->host_in = in;
+    ctx->host_out = out;
+    for (int i = 0; i < n; i++) ctx->host_ev[i] = ev[i];
+    ctx->host_ready = true;
+    return VJ_OK;
+}
+
+// vj_join_host with the probe side in chunks: the build side and the chunks are copied in
+// on one stream, each chunk is joined with the whole build side on the caller's stream as
+// soon as it has landed, and each chunk's pairs are copied out on a third stream while the
+// next chunk is joined. The host link carries both directions at once, so copies in, joins
+// and copies out overlap. R ⋈ S is the union of the R ⋈ S_i; each chunk's pairs follow the
+// previous chunks' in the output.
+int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, cudaStream_t st, int chunks, char *rk,
+                      char *rp, char *sk, char *sp, char *dpairs) {
+    VJ_TRY(host_streams(ctx));
+    const size_t kb = (size_t)r->key_words * 4, pb = (size_t)r->payload_bytes;
+    cudaEvent_t ev_start = ctx->host_ev[0], ev_in = ctx->host_ev[1], ev_out = ctx->host_ev[2];
+    cudaEvent_t *ev_s = ctx->host_ev + 3, *ev_j = ctx->host_ev + 3 + 16;
+    cudaStream_t in = ctx->host_in, out = ctx->host_out;
+    // chunk bounds on multiples of 64 rows keep every chunk's copy as aligned as the table
+    auto begin = [&](int i) { return i == chunks ? s->rows : (s->rows * (uint64_t)i / (uint64_t)chunks) & ~63ull; };
+    // copies in: the build side, then the chunks (ev_s[i]: chunk i and all before it landed)
+    VJ_CUDA(cudaEventRecord(ev_start, st));  // after whatever the caller queued before
+    cudaError_t e = cudaStreamWaitEvent(in, ev_start, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(out, ev_start, 0);
+    if (e == cudaSuccess) e = copy_in(rk, r->keys, r->rows * kb, in);
+    if (e == cudaSuccess) e = copy_in(rp, r->payloads, r->rows * pb, in);
+    for (int i = 0; i < chunks && e == cudaSuccess; i++) {
+        const uint64_t a = begin(i), n = begin(i + 1) - a;
+        e = copy_in(sk + a * kb, (const char *)s->keys + a * kb, n * kb, in);
+        if (e == cudaSuccess) e = copy_in(sp + a * pb, (const char *)s->payloads + a * pb, n * pb, in);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_s[i], in);
+    }
+    int status = e == cudaSuccess ? VJ_OK : cuda_error(e, "vj_join_host: copies to the device");
+    vj_table dr = *r;
+    dr.keys = rk;
+    dr.payloads = rp;
+    uint64_t off = 0, total = 0;
+    bool over = false;
+    for (int i = 0; i < chunks && status == VJ_OK; i++) {
+        const uint64_t a = begin(i);
+        vj_table ds = *s;
+        ds.keys = sk + a * kb;
+        ds.payloads = sp + a * pb;
+        ds.rows = begin(i + 1) - a;
+        e = cudaStreamWaitEvent(st, ev_s[i], 0);
+        if (e != cudaSuccess) {
+            status = cuda_error(e, "vj_join_host: stream order");
+            break;
+        }
+        // once the output is full the remaining chunks are counted only
+        const uint64_t room = over ? 0 : capacity - off;
+        uint64_t n = 0;
+        status = join_into(ctx, &dr, &ds, options, dpairs + off * 2 * pb, room, &n, st);
+        if (status != VJ_OK) break;
+        total += n;
+        if (over || n > room) {
+            over = true;
+            continue;
+        }
+        if (n) {
+            e = cudaEventRecord(ev_j[i], st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(out, ev_j[i], 0);
+            if (e == cudaSuccess) e = cudaMemcpyAsync((char *)h_pairs + off * 2 * pb, dpairs + off * 2 * pb, n * 2 * pb, cudaMemcpyDeviceToHost, out);
+            if (e != cudaSuccess) status = cuda_error(e, "vj_join_host: copy of pairs to the host");
+        }
+        off += n;
+    }
+    // the caller's stream takes over the completion of both copy streams, after an error
+    // too, so that no copy into the staging buffer outlives the call
+    e = cudaEventRecord(ev_in, in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_out, out);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_in, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_out, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (status != VJ_OK) return status;
+    if (e != cudaSuccess) return cuda_error(e, "vj_join_host: pipeline");
+    *count = total;
+    if (over) {
+        return set_error(VJ_ERR_CAPACITY, "vj_join_host: %llu pairs, capacity %llu", (unsigned long long)total, (unsigned long long)capacity);
+    }
+    return VJ_OK;
+}
+
+}  // namespace
+
 extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, vj_stream_t stream) {
     VJ_CHECK(ctx && count, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: null argument");
     VJ_TRY(check_table(r, "vj_join_host: r"));
@@ -1184,14 +1393,15 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     void *rk = c.take<char>(r->rows * kb), *rp = c.take<char>(r->rows * pb);
     void *sk = c.take<char>(s->rows * kb), *sp = c.take<char>(s->rows * pb);
     void *dpairs = c.take<char>((size_t)capacity * 2 * pb);
-    if (r->rows) {
-        VJ_CUDA(cudaMemcpyAsync(rk, r->keys, r->rows * kb, cudaMemcpyHostToDevice, st));
-        VJ_CUDA(cudaMemcpyAsync(rp, r->payloads, r->rows * pb, cudaMemcpyHostToDevice, st));
+    const int chunks = capacity > 0 ? host_chunks(r->rows, s->rows) : 1;
+    if (chunks > 1) {
+        VJ_CHECK(h_pairs != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: null output");
+        return join_host_chunked(ctx, r, s, options, h_pairs, capacity, count, st, chunks, (char *)rk, (char *)rp, (char *)sk, (char *)sp, (char *)dpairs);
     }
-    if (s->rows) {
-        VJ_CUDA(cudaMemcpyAsync(sk, s->keys, s->rows * kb, cudaMemcpyHostToDevice, st));
-        VJ_CUDA(cudaMemcpyAsync(sp, s->payloads, s->rows * pb, cudaMemcpyHostToDevice, st));
-    }
+    VJ_CUDA(copy_in(rk, r->keys, r->rows * kb, st));
+    VJ_CUDA(copy_in(rp, r->payloads, r->rows * pb, st));
+    VJ_CUDA(copy_in(sk, s->keys, s->rows * kb, st));
+    VJ_CUDA(copy_in(sp, s->payloads, s->rows * pb, st));
     vj_table dr = *r, ds = *s;
     dr.keys = rk;
     dr.payloads = rp;

@@ -333,6 +333,8 @@ extern "C" int vj_ctx_create(int device, uint64_t memory_budget_bytes, vj_ctx **
     c->owned_bytes = 0;
     c->stage = nullptr;
     c->stage_bytes = 0;
+    c->host_in = c->host_out = nullptr;
+    c->host_ready = false;
     c->profiling = false;
     c->events_ready = false;
     memset(&c->last, 0, sizeof(c->last));
@@ -388,6 +390,12 @@ extern "C" int vj_ctx_destroy(vj_ctx *ctx) {
         }
     }
     int st = vj_ctx_trim(ctx);
+    if (ctx->host_ready) {
+        cudaSetDevice(ctx->device);
+        for (cudaEvent_t e : ctx->host_ev) cudaEventDestroy(e);
+        cudaStreamDestroy(ctx->host_in);
+        cudaStreamDestroy(ctx->host_out);
+    }
     delete ctx;
     return st;
 }
