@@ -1158,11 +1158,12 @@ extern "C" int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashe
     return dispatch(in->key_words, in->payload_bytes, d_hashes_in ? hash_bits / 8 : 0, call);
 }
 
-// Copies n words from page-locked, mapped host memory to the device with SM loads, eight
-// in flight per thread. The copy engine's reads of host memory stall now and then on this
-// platform (1 GB taking 40-50 ms instead of 5 at times, with or without other GPU work),
-// while loads from a few SMs, which keep many host pages in flight at once, hold the link
-// rate of ~210 GB/s throughout.
+// Copies n words between the device and page-locked, mapped host memory with SM loads and
+// stores, eight loads in flight per thread. The copy engines' transfers to and from host
+// memory stall now and then on this platform (1 GB taking 40-60 ms instead of 5 at times,
+// with or without other GPU work), and a copy to the host can hold the calling thread until
+// it ends; loads and stores from a few SMs, which keep many host pages in flight at once,
+// hold the link rate (~210 GB/s in, ~190 out) throughout and never block the host.
 template <typename V>
 __global__ void __launch_bounds__(512) host_copy_kernel(const V *__restrict__ src, V *__restrict__ dst, size_t n) {
     constexpr int U = 8;
@@ -1202,12 +1203,9 @@ const char *mapped_host(const void *p, size_t bytes) {
     return (const char *)a.devicePointer;
 }
 
-// Host-to-device copy: SM loads for mapped page-locked memory, the copy engine otherwise
-// (pageable memory, which it stages itself).
-cudaError_t copy_in(void *dst, const void *src, size_t bytes, cudaStream_t stream) {
-    if (bytes == 0) return cudaSuccess;
-    const char *dsrc = mapped_host(src, bytes);
-    if (!dsrc) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+// SM copy of bytes between device addresses (one side a host mapping), in the widest words
+// that the addresses and the size allow.
+cudaError_t sm_copy(void *dst, const void *dsrc, size_t bytes, cudaStream_t stream) {
     const uintptr_t al = (uintptr_t)dsrc | (uintptr_t)dst | (uintptr_t)bytes;
     const dim3 grid(HOST_COPY_BLOCKS), block(512);
     if ((al & 15) == 0) {
@@ -1220,6 +1218,23 @@ cudaError_t copy_in(void *dst, const void *src, size_t bytes, cudaStream_t strea
         host_copy_kernel<uint8_t><<<grid, block, 0, stream>>>((const uint8_t *)dsrc, (uint8_t *)dst, bytes);
     }
     return cudaGetLastError();
+}
+
+// Host-to-device copy: SM loads for mapped page-locked memory, the copy engine otherwise
+// (pageable memory, which it stages itself).
+cudaError_t copy_in(void *dst, const void *src, size_t bytes, cudaStream_t stream) {
+    if (bytes == 0) return cudaSuccess;
+    const char *dsrc = mapped_host(src, bytes);
+    if (!dsrc) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+    return sm_copy(dst, dsrc, bytes, stream);
+}
+
+// Device-to-host copy: SM stores for mapped page-locked memory, the copy engine otherwise.
+cudaError_t copy_out(void *dst, const void *src, size_t bytes, cudaStream_t stream) {
+    if (bytes == 0) return cudaSuccess;
+    char *ddst = (char *)mapped_host(dst, bytes);
+    if (!ddst) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream);
+    return sm_copy(ddst, src, bytes, stream);
 }
 
 // A join into a caller's device buffer that is never reallocated, capacity 0 included
@@ -1267,11 +1282,11 @@ int host_streams(vj_ctx *ctx) {
     cudaStream_t in = nullptr, out = nullptr;
     cudaEvent_t ev[sizeof(ctx->host_ev) / sizeof(ctx->host_ev[0])] = {};
     const int n = (int)(sizeof(ev) / sizeof(ev[0]));
-    // copies in at the highest priority: their blocks are scheduled ahead of the joins'
+    // copies at the highest priority: their few blocks are scheduled ahead of the joins'
     int least = 0, greatest = 0;
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&in, cudaStreamNonBlocking, greatest);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&out, cudaStreamNonBlocking, greatest);
     for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         for (int i = 0; i < n; i++)
@@ -1344,7 +1359,7 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
         if (n) {
             e = cudaEventRecord(ev_j[i], st);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(out, ev_j[i], 0);
-            if (e == cudaSuccess) e = cudaMemcpyAsync((char *)h_pairs + off * 2 * pb, dpairs + off * 2 * pb, n * 2 * pb, cudaMemcpyDeviceToHost, out);
+            if (e == cudaSuccess) e = copy_out((char *)h_pairs + off * 2 * pb, dpairs + off * 2 * pb, n * 2 * pb, out);
             if (e != cudaSuccess) status = cuda_error(e, "vj_join_host: copy of pairs to the host");
         }
         off += n;
@@ -1424,7 +1439,7 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
         status = set_error(VJ_ERR_CAPACITY, "vj_join_host: %llu pairs, capacity %llu", (unsigned long long)res.count, (unsigned long long)capacity);
     } else if (res.count) {
         VJ_CHECK(h_pairs != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: null output");
-        cudaError_t e = cudaMemcpyAsync(h_pairs, res.pairs, res.count * 2 * pb, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = copy_out(h_pairs, res.pairs, res.count * 2 * pb, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) status = cuda_error(e, "vj_join_host: copy of pairs to the host");
     }
