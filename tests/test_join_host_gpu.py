@@ -135,3 +135,19 @@ def test_pinned_tables_at_any_alignment(vjlib, ctx, cuda, oracle, offset):
     cnt, want, _ = oracle.join(rk, g["r_pay"], sk, g["s_pay"])
     assert n == cnt == g["matches"]
     assert np.array_equal(sort_pairs(out[:n].numpy().view(np.uint32).astype(np.uint64)), want)
+
+
+def test_chunked_small_build_side(vjlib, ctx, cuda, oracle):
+    """A build side too small for a radix pass: each chunk is joined whole."""
+    rng = np.random.default_rng(55)
+    nr, ns = 1000, (1 << 23) + 5
+    rk = rng.integers(0, 3000, size=nr, dtype=np.uint64)
+    sk = rng.integers(0, 3000, size=ns, dtype=np.uint64)
+    rp = np.arange(nr, dtype=np.uint64)
+    sp = np.arange(ns, dtype=np.uint64)
+    cnt, _, _ = oracle.join(rk, rp, sk, sp)
+    want = device_join(vjlib, ctx, cuda, rk, rp, sk, sp, 2, 8)
+    assert want[0] == cnt
+    n, host = host_join(vjlib, ctx, cuda, rk, rp, sk, sp, 2, 8, cnt, True)
+    assert n == cnt
+    assert digest_of_host(vjlib, cuda, host, n, 8) == want[1]

@@ -409,10 +409,10 @@ struct vj_ctx {
     void *stage;            // device staging for vj_join_host
     size_t stage_bytes;
     // vj_join_host's pipeline: a stream for copies in, one for copies out, and its events
-    // (created on first use: call start, copies in done, copies out done, then one per
-    // probe-side chunk copied in and one per chunk joined, up to 16 chunks)
+    // (created on first use: call start, copies in done, copies out done, build side copied
+    // in, then one per probe-side chunk copied in and one per chunk joined, up to 16 chunks)
     cudaStream_t host_in, host_out;
-    cudaEvent_t host_ev[3 + 2 * 16];
+    cudaEvent_t host_ev[4 + 2 * 16];
     bool host_ready;
     bool profiling;
     cudaEvent_t events[16];  // created on first use

@@ -10,6 +10,7 @@
 #include "vj_l2_kernels.cuh"
 
 #include <cstring>
+#include <memory>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -1265,6 +1266,202 @@ int join_into(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_o
     return VJ_OK;
 }
 
+// ------------------------------------------------------------------ chunked probe side
+//
+// vj_join_host's pipeline joins the whole build side with one probe-side chunk at a time.
+// The build side is partitioned once, when it has landed; each chunk is partitioned on its
+// own (the plan's passes, one side per launch) and probed against the build side's
+// partitions. Partitions p of both sides hold the same hash range whichever launch made
+// them, so the items of partition p pair the build rows [r_begin[p], r_end[p]) with the
+// chunk's rows [s_begin[p], s_end[p]).
+
+struct ChunkJoiner {
+    virtual ~ChunkJoiner() = default;
+    // plans the join of r with a probe side of s_rows rows in chunks of at most max_chunk
+    // rows, and partitions r (r's rows must be on the device in stream order)
+    virtual int build(cudaStream_t stream) = 0;
+    // joins r with one chunk into (out, room); *count = all its pairs (synchronises)
+    virtual int probe(const vj_table &chunk, void *out, uint64_t room, uint64_t *count, cudaStream_t stream) = 0;
+};
+
+// Workspace of one side's passes.
+struct SideBufs {
+    void *rows[2] = {nullptr, nullptr};  // partition buffer of each pass
+    uint16_t *bids = nullptr;             // pass-2 buckets written by pass 1
+    PassBufs pb[2] = {};
+};
+
+template <int KW, int PB, int HS>
+struct ChunkJoinerT final : ChunkJoiner {
+    using L = Layout<KW, PB, HS>;
+    vj_ctx *ctx;
+    vj_table r;
+    uint64_t s_rows;
+    uint32_t max_chunk;
+    HashSpec hs;
+    const vj_join_options *opt;
+    Plan pl;
+    bool direct = false;  // no radix pass: each chunk is joined whole
+    int np = 1;
+    SideBufs rb, sb;
+    const uint32_t *r_begin = nullptr, *r_end = nullptr;
+    uint32_t *item_begin = nullptr, *ticket = nullptr, *error = nullptr;
+    uint4 *item_desc = nullptr;
+    unsigned long long *plan_blocks = nullptr, *out_count = nullptr;
+    uint64_t item_cap = 0;
+
+    int units(int pass) const { return ctx->info.sms * 64 + (pass == 0 ? 1 : (1 << pl.bits[0])); }
+
+    void carve_side(Carver &c, uint32_t rows, SideBufs *b) const {
+        for (int pass = 0; pass < 2; pass++) b->rows[pass] = pl.passes > pass ? c.take<char>((size_t)rows * L::STRIDE + 64) : nullptr;
+        b->bids = pl.passes >= 2 ? c.take<uint16_t>((size_t)rows + 8) : nullptr;
+        for (int pass = 0; pass < pl.passes; pass++) b->pb[pass] = carve_pass(c, pass == 0 ? 1 : 1 << pl.bits[0], 1 << pl.bits[pass], units(pass));
+    }
+
+    void layout(Carver &c) {
+        carve_side(c, (uint32_t)r.rows, &rb);
+        carve_side(c, max_chunk, &sb);
+        item_begin = c.take<uint32_t>((size_t)np + 2);
+        plan_blocks = c.take<unsigned long long>(((size_t)np + PLAN_BLOCK - 1) / PLAN_BLOCK);
+        item_desc = c.take<uint4>(item_cap);
+        ticket = c.take<uint32_t>(1);
+        out_count = c.take<unsigned long long>(1);
+        error = c.take<uint32_t>(1);
+    }
+
+    // The plan's passes over one table; its partitions are rows [begin[p], end[p]) of the
+    // last pass's buffer.
+    int partition(const void *keys, const void *pay, uint32_t rows, const SideBufs &b, cudaStream_t stream, const uint32_t **begin, const uint32_t **end) {
+        const uint32_t *seg_begin = nullptr, *seg_end = nullptr;
+        int Q = 1, consumed = 0;
+        for (int pass = 0; pass < pl.passes; pass++) {
+            PassParams P{};
+            P.side[0].keys_in = keys;
+            P.side[0].pay_in = pay;
+            P.side[0].hash_in = nullptr;
+            P.side[0].rows_in = pass > 0 ? b.rows[pass - 1] : nullptr;
+            P.side[0].rows_out = b.rows[pass];
+            P.side[0].rows = rows;
+            P.side[0].bid_out = pass == 0 && pl.passes >= 2 ? b.bids : nullptr;
+            P.side[0].bid_in = pass == 1 ? b.bids : nullptr;
+            P.next_shift = 64 - (pl.bits[0] + pl.bits[1]);
+            P.next_bits = pl.bits[1];
+            P.nsides = 1;
+            P.Q = Q;
+            P.seg_begin = seg_begin;
+            P.seg_end = seg_end;
+            P.bits = pl.bits[pass];
+            consumed += pl.bits[pass];
+            P.shift = 64 - consumed;
+            P.hs = hs;
+            P.max_units = units(pass);
+            P.min_unit_rows = 4096;
+            P.error = error;
+            if (pass == 0) {
+                VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, pass, P, b.pb[0], stream)));
+            } else {
+                VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, pass, P, b.pb[1], stream)));
+            }
+            seg_begin = b.pb[pass].part_begin;
+            seg_end = b.pb[pass].part_end;
+            Q <<= pl.bits[pass];
+        }
+        *begin = seg_begin;
+        *end = seg_end;
+        return VJ_OK;
+    }
+
+    int build(cudaStream_t stream) override {
+        pl = make_plan<KW, PB, HS>(r.rows, s_rows, ctx->info, opt, VJ_TABLES_SHARED);
+        if (pl.passes == 0) {
+            direct = true;
+            return VJ_OK;
+        }
+        np = pl.passes == 1 ? 1 << pl.bits[0] : 1 << (pl.bits[0] + pl.bits[1]);
+        item_cap = (uint64_t)np + max_chunk / pl.schunk + r.rows / pl.rcap + 4096;
+        Carver dry;
+        layout(dry);
+        void *ws = nullptr;
+        VJ_TRY(workspace_reserve(ctx, dry.off + 256, stream, &ws));
+        Carver c;
+        c.base = (char *)ws;
+        layout(c);
+        VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
+        return partition(r.keys, r.payloads, (uint32_t)r.rows, rb, stream, &r_begin, &r_end);
+    }
+
+    int probe(const vj_table &chunk, void *out, uint64_t room, uint64_t *count, cudaStream_t stream) override {
+        *count = 0;
+        if (direct) return join_into(ctx, &r, &chunk, opt, out, room, count, stream);
+        if (chunk.rows == 0 || r.rows == 0) return VJ_OK;
+        ctx->launches = 0;
+        const uint32_t *s_begin = nullptr, *s_end = nullptr;
+        VJ_TRY(partition(chunk.keys, chunk.payloads, (uint32_t)chunk.rows, sb, stream, &s_begin, &s_end));
+        ProbeParams Pq{};
+        Pq.r_keys = r.keys;
+        Pq.r_pay = r.payloads;
+        Pq.s_keys = chunk.keys;
+        Pq.s_pay = chunk.payloads;
+        Pq.r_rows_in = rb.rows[pl.passes - 1];
+        Pq.s_rows_in = sb.rows[pl.passes - 1];
+        Pq.r_begin = r_begin;
+        Pq.r_end = r_end;
+        Pq.s_begin = s_begin;
+        Pq.s_end = s_end;
+        Pq.r_rows = (uint32_t)r.rows;
+        Pq.s_rows = (uint32_t)chunk.rows;
+        Pq.np = np;
+        Pq.rcap = pl.rcap;
+        Pq.schunk = pl.schunk;
+        Pq.outcap = pl.outcap;
+        Pq.sub_rows = pl.sub;
+        Pq.slot_shift = 64 - (pl.bits[0] + pl.bits[1]) - 14;
+        Pq.item_begin = item_begin;
+        Pq.item_desc = item_desc;
+        Pq.item_cap = (uint32_t)(item_cap < 0xffffffffull ? item_cap : 0xffffffffull);
+        Pq.ticket = ticket;
+        Pq.out_count = out_count;
+        Pq.hs = hs;
+        Pq.error = error;
+        Pq.joins = 1;
+        Pq.out = out;
+        Pq.capacity = room;
+        JoinRun run;
+        run.probe = Pq;
+        run.plan_blocks = plan_blocks;
+        run.d_out_count = out_count;
+        run.d_error = error;
+        VJ_TRY((probe_setup<KW, PB, HS, true, false>(ctx, pl, &run)));
+        VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
+        uint32_t flags = 0;
+        VJ_TRY(read_count(run, stream, count, &flags));
+        VJ_TRY(check_flags(flags));
+        finish_profile(ctx, pl, r.rows, chunk.rows, *count);
+        return VJ_OK;
+    }
+};
+
+struct MakeChunkJoiner {
+    vj_ctx *ctx;
+    const vj_table *r;
+    uint64_t s_rows;
+    uint32_t max_chunk;
+    const vj_join_options *opt;
+    std::unique_ptr<ChunkJoiner> *out;
+    template <int KW, int PB, int HS>
+    int run() {
+        auto j = std::make_unique<ChunkJoinerT<KW, PB, HS>>();
+        j->ctx = ctx;
+        j->r = *r;
+        j->s_rows = s_rows;
+        j->max_chunk = max_chunk;
+        j->hs = spec_from(opt, 1);
+        j->opt = opt;
+        *out = std::move(j);
+        return VJ_OK;
+    }
+};
+
 // Probe-side chunks of vj_join_host's pipeline. A chunk's join (the whole build side and
 // the chunk) takes about as long as the copy of one build side's worth of probe rows, so
 // chunks of about |R| rows keep the link busy; 1 (no pipeline) for a probe side under
@@ -1312,8 +1509,8 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
                       char *rp, char *sk, char *sp, char *dpairs) {
     VJ_TRY(host_streams(ctx));
     const size_t kb = (size_t)r->key_words * 4, pb = (size_t)r->payload_bytes;
-    cudaEvent_t ev_start = ctx->host_ev[0], ev_in = ctx->host_ev[1], ev_out = ctx->host_ev[2];
-    cudaEvent_t *ev_s = ctx->host_ev + 3, *ev_j = ctx->host_ev + 3 + 16;
+    cudaEvent_t ev_start = ctx->host_ev[0], ev_in = ctx->host_ev[1], ev_out = ctx->host_ev[2], ev_r = ctx->host_ev[3];
+    cudaEvent_t *ev_s = ctx->host_ev + 4, *ev_j = ctx->host_ev + 4 + 16;
     cudaStream_t in = ctx->host_in, out = ctx->host_out;
     // chunk bounds on multiples of 64 rows keep every chunk's copy as aligned as the table
     auto begin = [&](int i) { return i == chunks ? s->rows : (s->rows * (uint64_t)i / (uint64_t)chunks) & ~63ull; };
@@ -1323,8 +1520,11 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
     if (e == cudaSuccess) e = cudaStreamWaitEvent(out, ev_start, 0);
     if (e == cudaSuccess) e = copy_in(rk, r->keys, r->rows * kb, in);
     if (e == cudaSuccess) e = copy_in(rp, r->payloads, r->rows * pb, in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_r, in);
+    uint32_t max_chunk = 0;
     for (int i = 0; i < chunks && e == cudaSuccess; i++) {
         const uint64_t a = begin(i), n = begin(i + 1) - a;
+        max_chunk = std::max<uint32_t>(max_chunk, (uint32_t)n);
         e = copy_in(sk + a * kb, (const char *)s->keys + a * kb, n * kb, in);
         if (e == cudaSuccess) e = copy_in(sp + a * pb, (const char *)s->payloads + a * pb, n * pb, in);
         if (e == cudaSuccess) e = cudaEventRecord(ev_s[i], in);
@@ -1333,6 +1533,16 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
     vj_table dr = *r;
     dr.keys = rk;
     dr.payloads = rp;
+    // the build side is partitioned once, as soon as it has landed
+    std::unique_ptr<ChunkJoiner> joiner;
+    if (status == VJ_OK) {
+        MakeChunkJoiner mk{ctx, &dr, s->rows, max_chunk, tuned_options(ctx, r, s, options), &joiner};
+        status = dispatch(r->key_words, r->payload_bytes, 0, mk);
+    }
+    if (status == VJ_OK) {
+        e = cudaStreamWaitEvent(st, ev_r, 0);
+        status = e == cudaSuccess ? joiner->build(st) : cuda_error(e, "vj_join_host: stream order");
+    }
     uint64_t off = 0, total = 0;
     bool over = false;
     for (int i = 0; i < chunks && status == VJ_OK; i++) {
@@ -1349,7 +1559,7 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
         // once the output is full the remaining chunks are counted only
         const uint64_t room = over ? 0 : capacity - off;
         uint64_t n = 0;
-        status = join_into(ctx, &dr, &ds, options, dpairs + off * 2 * pb, room, &n, st);
+        status = joiner->probe(ds, dpairs + off * 2 * pb, room, &n, st);
         if (status != VJ_OK) break;
         total += n;
         if (over || n > room) {
