@@ -671,18 +671,27 @@ void finish_profile(vj_ctx *ctx, const Plan &pl, uint64_t nr, uint64_t ns, uint6
     p.ms_total = ms(pl.passes ? PM_PASS0 : PM_PROBE_BEGIN, PM_PROBE_END);
 }
 
+// Match count and error flags of a probe, stored by one thread into page-locked host memory
+// (the copy engines' small copies to the host stalled now and then for tens of ms).
+__global__ void read_count_kernel(const unsigned long long *count, const uint32_t *error, volatile unsigned long long *host) {
+    host[0] = *count;
+    host[1] = *error;
+}
+
 // Match count and the kernels' error flags of the probe just launched (synchronises).
-int read_count(const JoinRun &run, cudaStream_t stream, uint64_t *count, uint32_t *flags) {
-    static thread_local unsigned long long *pinned = nullptr;
+int read_count(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream, uint64_t *count, uint32_t *flags) {
+    static thread_local unsigned long long *pinned = nullptr, *mapped = nullptr;
     if (!pinned) {
-        VJ_CUDA(cudaMallocHost(&pinned, 2 * sizeof(unsigned long long)));
+        VJ_CUDA(cudaHostAlloc((void **)&pinned, 2 * sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable));
+        VJ_CUDA(cudaHostGetDevicePointer((void **)&mapped, pinned, 0));
     }
-    pinned[1] = 0;
-    VJ_CUDA(cudaMemcpyAsync(&pinned[0], run.d_out_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
-    VJ_CUDA(cudaMemcpyAsync(&pinned[1], run.d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    read_count_kernel<<<1, 1, 0, stream>>>(run.d_out_count, run.d_error, mapped);
+    VJ_CUDA(cudaGetLastError());
+    ctx->launches += 1;
     VJ_CUDA(cudaStreamSynchronize(stream));
-    *flags = (uint32_t)pinned[1];
-    *count = pinned[0];
+    const volatile unsigned long long *h = pinned;
+    *count = h[0];
+    *flags = (uint32_t)h[1];
     return VJ_OK;
 }
 
@@ -705,7 +714,7 @@ int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
     run->probe.capacity = capacity;
     VJ_TRY((launch_probe<KW, PB, HS>(ctx, *run, stream)));
     uint32_t flags = 0;
-    VJ_TRY(read_count(*run, stream, count, &flags));
+    VJ_TRY(read_count(ctx, *run, stream, count, &flags));
     if ((flags & 8u) && pl.tables == VJ_TABLES_L2) {
         VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, VJ_TABLES_SHARED, out, capacity, stream, run, plan, count)));
         plan->fallbacks += 1;
@@ -755,7 +764,7 @@ int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
         VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
         uint64_t again = 0;
         uint32_t flags = 0;
-        VJ_TRY(read_count(run, stream, &again, &flags));
+        VJ_TRY(read_count(ctx, run, stream, &again, &flags));
         VJ_TRY(check_flags(flags));
         VJ_CHECK(again == count, VJ_ERR_DEVICE, "second probe gave %llu pairs, first %llu", (unsigned long long)again, (unsigned long long)count);
     }
@@ -1182,9 +1191,11 @@ __global__ void __launch_bounds__(512) host_copy_kernel(const V *__restrict__ sr
 
 namespace {
 
-// Blocks of host_copy_kernel: 16 x 512 threads x 8 loads of 16 bytes keep 1 MB in flight,
-// enough for the link, and leave the other SMs to the joins they overlap.
-constexpr int HOST_COPY_BLOCKS = 16;
+// Blocks of host_copy_kernel: 16 x 512 threads x 8 loads of 16 bytes (1 MB in flight) fill
+// the link alone; beside the joins they overlap, 32 keep more of it (the 2^27 x 2^29 join
+// from host tables: 71.6 ms with 32, 75.7 with 16, no better with 64), and the other SMs
+// stay with the joins.
+constexpr int HOST_COPY_BLOCKS = 32;
 
 // Device address of host memory [p, p + bytes) that the GPU can load from (page-locked and
 // mapped, both ends in the same mapping), or null.
@@ -1434,7 +1445,7 @@ struct ChunkJoinerT final : ChunkJoiner {
         VJ_TRY((probe_setup<KW, PB, HS, true, false>(ctx, pl, &run)));
         VJ_TRY((launch_probe<KW, PB, HS>(ctx, run, stream)));
         uint32_t flags = 0;
-        VJ_TRY(read_count(run, stream, count, &flags));
+        VJ_TRY(read_count(ctx, run, stream, count, &flags));
         VJ_TRY(check_flags(flags));
         finish_profile(ctx, pl, r.rows, chunk.rows, *count);
         return VJ_OK;
@@ -1512,8 +1523,13 @@ int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const v
     cudaEvent_t ev_start = ctx->host_ev[0], ev_in = ctx->host_ev[1], ev_out = ctx->host_ev[2], ev_r = ctx->host_ev[3];
     cudaEvent_t *ev_s = ctx->host_ev + 4, *ev_j = ctx->host_ev + 4 + 16;
     cudaStream_t in = ctx->host_in, out = ctx->host_out;
-    // chunk bounds on multiples of 64 rows keep every chunk's copy as aligned as the table
-    auto begin = [&](int i) { return i == chunks ? s->rows : (s->rows * (uint64_t)i / (uint64_t)chunks) & ~63ull; };
+    // Chunk i weighs 2 (chunks + 1) - i: later chunks are smaller, so the join and the copy
+    // out left after the last chunk has landed are short (4 chunks of 29, 26, 24 and 21 % of
+    // the probe side: 71.6 ms for the 2^27 x 2^29 join, 4 equal chunks 73.9 ms). Bounds on
+    // multiples of 64 rows keep every chunk's copy as aligned as the table.
+    const uint64_t C = (uint64_t)chunks;
+    auto weight_below = [&](uint64_t i) -> uint64_t { return i * (4 * (C + 1) - i + 1) / 2; };
+    auto begin = [&](int i) -> uint64_t { return i == chunks ? s->rows : (s->rows * weight_below((uint64_t)i) / weight_below(C)) & ~(uint64_t)63; };
     // copies in: the build side, then the chunks (ev_s[i]: chunk i and all before it landed)
     VJ_CUDA(cudaEventRecord(ev_start, st));  // after whatever the caller queued before
     cudaError_t e = cudaStreamWaitEvent(in, ev_start, 0);
