@@ -765,6 +765,19 @@ def main():
         dist.barrier()
     value = job_rate(nr + ns, args.steps, world, total_ms)
 
+    # p50/p99 over at least LATENCY_SAMPLES joins: the timed steps, then more joins after
+    # the timed region (they do not enter `value`)
+    lat_ms = list(step_ms)
+    extra = max(0, LATENCY_SAMPLES - args.steps)
+    if extra:
+        lev = [torch.cuda.Event(enable_timing=True) for _ in range(extra + 1)]
+        lev[0].record(stream)
+        for i in range(extra):
+            step()
+            lev[i + 1].record(stream)
+        torch.cuda.synchronize()
+        lat_ms += [lev[i].elapsed_time(lev[i + 1]) for i in range(extra)]
+
     # ---- roofline of the dominant kernel (stage events recorded by the library)
     peak, peak_src = measured_peak()
     w_k, w_p = cfg["key_bytes"], cfg["payload_bytes"]
@@ -846,18 +859,6 @@ def main():
     if tuned_opts is not None:
         cfg["tuned_plan"] = vj.options_dict(tuned_opts)
         cfg["tuner_best_ms"] = tuned_ms
-    # p50/p99 over at least LATENCY_SAMPLES joins: the timed steps, then more joins after
-    # the timed region (they do not enter `value`)
-    lat_ms = list(step_ms)
-    extra = max(0, LATENCY_SAMPLES - args.steps)
-    if extra:
-        lev = [torch.cuda.Event(enable_timing=True) for _ in range(extra + 1)]
-        lev[0].record(stream)
-        for i in range(extra):
-            step()
-            lev[i + 1].record(stream)
-        torch.cuda.synchronize()
-        lat_ms += [lev[i].elapsed_time(lev[i + 1]) for i in range(extra)]
     lat = sorted(lat_ms)
 
     def pct(q):
