@@ -10,7 +10,7 @@ max(n / 256, 1) blocks; custom_n_mult_xor_shift gets rounds = 2, hash.cu:526).
 This pins every golden vector to the reference's compiled code on the GPU, including the
 elements whose value rests on a *_shift variant's out-of-range shift amount.
 
-    python oracle/ref_gpu_check.py [--out gpurun_out/ref_gpu_check.json]
+    python oracle/ref_gpu_check.py [--out FILE.json]
 
 Exit status 0 when every vector matches, 1 on a mismatch, 2 when the cubins are absent.
 """

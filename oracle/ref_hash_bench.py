@@ -6,7 +6,7 @@ oracle/ref_build.sh -- and run with its own dispatcher's grid (hash.cu:507-509: 
 threads, max(n / elements_per_thread / 256, 1) blocks, elements_per_thread = 1). Both
 outputs are compared element for element before timing.
 
-    python oracle/ref_hash_bench.py [--keys-log2 30] [--out gpurun_out/ref_hash_bench.json]
+    python oracle/ref_hash_bench.py [--keys-log2 30] [--out FILE.json]
 
 Exit status 0 on success, 2 when the cubin is absent.
 """
