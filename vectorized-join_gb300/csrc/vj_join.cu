@@ -678,13 +678,31 @@ __global__ void read_count_kernel(const unsigned long long *count, const uint32_
     host[1] = *error;
 }
 
+// Per host thread: the page-locked words read_count_kernel stores into, freed when the
+// thread ends.
+struct CountWords {
+    unsigned long long *host = nullptr, *mapped = nullptr;
+    ~CountWords() {
+        if (host) cudaFreeHost(host);
+    }
+};
+
 // Match count and the kernels' error flags of the probe just launched (synchronises).
 int read_count(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream, uint64_t *count, uint32_t *flags) {
-    static thread_local unsigned long long *pinned = nullptr, *mapped = nullptr;
-    if (!pinned) {
-        VJ_CUDA(cudaHostAlloc((void **)&pinned, 2 * sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable));
-        VJ_CUDA(cudaHostGetDevicePointer((void **)&mapped, pinned, 0));
+    static thread_local CountWords words;
+    if (!words.host) {
+        unsigned long long *h = nullptr;
+        VJ_CUDA(cudaHostAlloc((void **)&h, 2 * sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable));
+        unsigned long long *d = nullptr;
+        const cudaError_t e = cudaHostGetDevicePointer((void **)&d, h, 0);
+        if (e != cudaSuccess) {
+            cudaFreeHost(h);
+            return cuda_error(e, "read_count: mapped host words");
+        }
+        words.host = h;
+        words.mapped = d;
     }
+    unsigned long long *pinned = words.host, *mapped = words.mapped;
     read_count_kernel<<<1, 1, 0, stream>>>(run.d_out_count, run.d_error, mapped);
     VJ_CUDA(cudaGetLastError());
     ctx->launches += 1;
