@@ -1,5 +1,6 @@
-"""`bench.py --impl reference` (the CPU oracle port on the host's cores) runs without a GPU
-and prints one JSON line with the bench contract's keys."""
+"""`bench.py --impl reference` at its default size (the 2^27 x 2^29 configuration; the CPU
+oracle port joins a bounded sample of it on the host's cores) runs without a GPU and prints exactly one JSON line with the contract's keys. The
+`--small` form and the other ranks are covered in test_bench_ranks.py."""
 from __future__ import annotations
 
 import json
@@ -11,9 +12,10 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def run_reference(env_extra=None):
+def run_reference():
     env = dict(os.environ)
-    env.update(env_extra or {})
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
     p = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert p.returncode == 0, p.stderr[-2000:]
     return [l for l in p.stdout.splitlines() if l.strip()]
@@ -31,7 +33,3 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
-
-def test_reference_arm_other_ranks_print_nothing():
-    lines = run_reference({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
-    assert lines == []
