@@ -67,3 +67,24 @@ def test_join_argument_validation_without_gpu(vjlib):
     assert lib.vj_generate_join(1, 3, 8, 1, 1, 0, None, None, None, None, None) == vjlib.VJ_ERR_INVALID_ARGUMENT
     assert lib.vj_ctx_destroy(None) == 0
     assert lib.vj_ctx_memory_in_use(None) == 0
+
+
+def test_host_batch_and_tune_argument_validation_without_gpu(vjlib):
+    lib = vjlib.load()
+    t = vjlib.VjTable(None, None, 0, 2, 8)
+    n = ctypes.c_uint64(7)
+    # null context / count are reported before any device work
+    assert lib.vj_join_host(None, ctypes.byref(t), ctypes.byref(t), None, None, 0, ctypes.byref(n), None) == vjlib.VJ_ERR_INVALID_ARGUMENT
+    assert lib.vj_join_host(None, ctypes.byref(t), ctypes.byref(t), None, None, 0, None, None) == vjlib.VJ_ERR_INVALID_ARGUMENT
+    assert lib.vj_join_batch(None, ctypes.byref(t), ctypes.byref(t), 1, None, None, 0, None, None, None, 0, None, None, None) == vjlib.VJ_ERR_INVALID_ARGUMENT
+    assert lib.vj_tune(None, ctypes.byref(t), ctypes.byref(t), None, None, 0, 0, None, None, None) == vjlib.VJ_ERR_INVALID_ARGUMENT
+    assert "null" in vjlib.last_error()
+
+
+def test_join_options_round_trip(vjlib):
+    o = vjlib.options(passes=2, radix_bits=(8, 9), build_rows=1024, tables="shared")
+    d = vjlib.options_dict(o)
+    assert d["tables"] == "shared" and d["passes"] == 2 and d["radix_bits"] == [8, 9] and d["build_rows"] == 1024
+    a = vjlib.options_dict(vjlib.options())
+    assert a["tables"] == "auto" and a["passes"] == "auto"
+    assert vjlib.options_dict(vjlib.options(tables="l2"))["tables"] == "l2"
