@@ -127,9 +127,8 @@ typedef struct vj_profile {
     float ms_total;             /* first partition launch to the end of the probe */
     uint64_t rows[2];           /* |R|, |S| */
     uint64_t matches;
-    int32_t tables;             /* VJ_TABLES_SHARED or VJ_TABLES_L2: where build tables lived */
-    int32_t fallbacks;          /* L2-table joins redone with shared-memory tables (long
-                                   duplicate clusters) */
+    int32_t tables;             /* VJ_TABLES_SHARED: where build tables lived */
+    int32_t fallbacks;          /* always 0 (kept for layout compatibility) */
 } vj_profile;
 
 enum { VJ_TABLES_SHARED = 0, VJ_TABLES_L2 = 1 };
@@ -208,11 +207,11 @@ VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes
 
 /* Join options (JoinConfig, src/join/join_provider.cuh:108-122). A zero-initialised struct
  * means "automatic": FNV-1a, 64-bit hash, passes, radix bits and table size from the tuner. */
-/* flags: VJ_JOIN_FIXED_PASSES takes passes and radix_bits as given; VJ_JOIN_SHARED_TABLES
- * and VJ_JOIN_L2_TABLES pick where the build tables live: shared-memory tables per build
- * chunk of <= 8192 rows after up to two radix passes (the default), or L2-resident tables
- * per partition of ~2^17 build rows after one pass (radix_bits[0], when fixed, is that
- * pass's width; build_rows caps the rows per table). */
+/* flags: VJ_JOIN_FIXED_PASSES takes passes and radix_bits as given. Build tables are
+ * shared-memory tables per build chunk of <= 8192 rows after up to two radix passes;
+ * VJ_JOIN_SHARED_TABLES names that explicitly. VJ_JOIN_L2_TABLES (L2-resident tables per
+ * partition after one pass) is no longer offered: it was slower than shared-memory tables
+ * on every measured shape, and a join that asks for it returns VJ_ERR_UNSUPPORTED. */
 enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4 };
 typedef struct vj_join_options {
     int32_t hash_algo;      /* VJ_HASH_*: the hash the partitions are cut from */
@@ -223,9 +222,13 @@ typedef struct vj_join_options {
     int32_t build_rows;     /* build rows per shared-memory table, rounded up to a power of
                                two and capped by shared memory; 0 = largest that fits */
     int32_t probe_rows;     /* probe rows per work item; 0 = automatic */
-    int32_t probe_threads;  /* threads per probe block (64..512, multiple of 32); 0 = automatic */
-    int32_t probe_sub_rows; /* probe rows per bulk copy (32..2048); 0 = automatic */
-    int32_t reserved[4];
+    int32_t probe_threads;  /* threads per probe block (64..1024, multiple of 32; one warp
+                               fetches work and flushes pairs, the others build and probe);
+                               0 = automatic (1024) */
+    int32_t probe_sub_rows; /* unused (kept for layout compatibility) */
+    int32_t table_load_pct; /* largest load of a build table in percent (50, 25 or 12: table
+                               slots per build row 2, 4 or 8); 0 = automatic (50) */
+    int32_t reserved[3];
 } vj_join_options;
 
 /* Join output. If pairs != NULL and capacity > 0 on entry, the caller owns the buffer (device

@@ -88,3 +88,6 @@ def test_join_options_round_trip(vjlib):
     a = vjlib.options_dict(vjlib.options())
     assert a["tables"] == "auto" and a["passes"] == "auto"
     assert vjlib.options_dict(vjlib.options(tables="l2"))["tables"] == "l2"
+    t = vjlib.options_dict(vjlib.options(probe_threads=256, table_load_pct=25, probe_rows=4096))
+    assert t["probe_threads"] == 256 and t["table_load_pct"] == 25 and t["probe_rows"] == 4096
+    assert ctypes.sizeof(vjlib.VjJoinOptions) == 56  # include/vj.h layout (unchanged by table_load_pct)

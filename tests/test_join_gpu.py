@@ -149,6 +149,37 @@ def test_duplicate_build_keys_grow_library_output(vjlib, ctx, cuda, oracle):
     assert e.value.status == vjlib.VJ_ERR_CAPACITY
 
 
+def test_probe_shapes_vs_oracle(vjlib, ctx, cuda, oracle):
+    """Probe block sizes, table loads and build/probe chunk sizes (several items per
+    partition, items with more probe rows than one round) give the oracle's pairs."""
+    rng = np.random.default_rng(12)
+    nr, ns = 40_000, 300_000
+    rk = rng.permutation(np.arange(nr, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+    pick = rng.integers(0, 2 * nr, size=ns)
+    sk = np.where(pick < nr, rk[np.minimum(pick, nr - 1)], pick.astype(np.uint64) + np.uint64(1 << 40))
+    rp = np.arange(nr, dtype=np.uint64)
+    sp = np.arange(ns, dtype=np.uint64)
+    cnt, want, _ = oracle.join(rk, rp, sk, sp)
+    for opts in (
+        vjlib.options(probe_threads=64),
+        vjlib.options(probe_threads=288),
+        vjlib.options(probe_threads=1024, table_load_pct=25),
+        vjlib.options(table_load_pct=12),
+        vjlib.options(passes=1, radix_bits=(3, 0), build_rows=512, probe_rows=20_000),
+        vjlib.options(passes=2, radix_bits=(2, 2), probe_rows=9000),
+    ):
+        count, got = gpu_join(vjlib, ctx, cuda, rk, rp, sk, sp, opts, capacity=cnt)
+        assert count == cnt, vjlib.options_dict(opts)
+        assert np.array_equal(sort_pairs(got), want), vjlib.options_dict(opts)
+
+
+def test_l2_tables_flag_refused(vjlib, ctx, cuda):
+    one = np.array([5], np.uint64)
+    with pytest.raises(vjlib.VjError) as e:
+        gpu_join(vjlib, ctx, cuda, one, one, one, one, vjlib.options(tables="l2"))
+    assert e.value.status == vjlib.VJ_ERR_UNSUPPORTED
+
+
 def test_empty_and_single(vjlib, ctx, cuda):
     e = np.zeros(0, np.uint64)
     one = np.array([5], np.uint64)
@@ -227,7 +258,7 @@ def test_generator_matches_oracle(vjlib, cuda, oracle):
         assert vjlib.generate_join_expect(42, nr, ns, thr) == oracle.gen_join_expect(42, nr, ns, 0.5)
 
 
-@pytest.mark.parametrize("tables", ["auto", "shared", "l2"])
+@pytest.mark.parametrize("tables", ["auto", "shared"])
 @pytest.mark.parametrize(
     "name,kb,pb,nr,ns,ratio",
     [
@@ -254,8 +285,7 @@ def test_full_size_count_and_digest(vjlib, ctx, cuda, name, kb, pb, nr, ns, rati
     opts = vjlib.options(tables=tables)
     res = ctx.join(vjlib.table(rk, rp, nr, kb // 4, pb), vjlib.table(sk, sp, ns, kb // 4, pb), opts, out=out, capacity=cap)
     assert res.count == want[0], name
-    if tables != "auto":
-        assert ctx.last_profile().tables == (1 if tables == "l2" else 0)
+    assert ctx.last_profile().tables == 0
     assert vjlib.pairs_digest(out, res.count, pb) == (want[1], want[2]), name
     del rk, sk, rp, sp, out
     torch.cuda.empty_cache()

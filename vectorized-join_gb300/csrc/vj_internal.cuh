@@ -274,10 +274,17 @@ struct PayloadType<8> {
 // ------------------------------------------------------------------ bulk copies (TMA engine)
 //
 // 1-D global->shared copies by the Blackwell bulk-copy (TMA) engine, completing on an
-// mbarrier with a transaction count. Every wait is bounded: after WAIT_LIMIT polls the
-// caller gets `false` and is expected to flag the error and leave.
+// mbarrier with a transaction count, and shared->global bulk stores. Every wait is bounded:
+// after WAIT_NS nanoseconds of polling the caller gets `false` and is expected to flag the
+// error and leave (a legitimate wait lasts microseconds).
 
-constexpr uint32_t WAIT_LIMIT = 1u << 24;
+constexpr uint64_t WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -307,11 +314,38 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return done != 0;
 }
 
+// Waits for the phase of `bar` with the given parity to complete; false once WAIT_NS have
+// passed without it.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
-        if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 16; i++) {
+            if (mbar_try_wait(bar, parity)) return true;
+        }
+        if (global_ns() - t0 > WAIT_NS) return false;
     }
-    return false;
+}
+
+// Plain arrival (release at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Named barrier `id` over `count` threads (a multiple of 32) that also ORs a predicate:
+// every participating thread gets true if any passed true.
+__device__ __forceinline__ bool bar_or(uint32_t id, uint32_t count, bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, %2, %3, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 // dst, src 16-byte aligned; bytes a multiple of 16.
@@ -319,6 +353,17 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+
+// Shared->global bulk store (dst, src 16-byte aligned; bytes a multiple of 16), tracked by
+// the issuing thread's bulk groups.
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// The issuing thread's bulk stores have read their shared-memory sources.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// The issuing thread's bulk stores are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Prefetch [src, src + bytes) into L2 through the bulk-copy engine (no completion to wait
 // for; src 16-byte aligned, bytes a multiple of 16).

@@ -7,7 +7,7 @@
 // buffer per pair (:694). Here one stream carries a fixed sequence of launches; every
 // decision that depends on data (unit split, partition bounds, work items) is made on
 // the device, and the host synchronises once, to read the match count.
-#include "vj_l2_kernels.cuh"
+#include "vj_join_kernels.cuh"
 
 #include <cstring>
 #include <memory>
@@ -40,20 +40,11 @@ struct Plan {
     int bits[2] = {0, 0};
     uint32_t rcap = 2048;     // build rows per table
     uint32_t schunk = 8192;   // probe rows per work item
-    uint32_t sub = 1024;      // probe rows per bulk copy
-    uint32_t outcap = 1536;   // staged output pairs per block
-    int threads = PROBE_THREADS;  // probe block size
+    uint32_t tmul = 2;        // table slots per build row (load <= 1/tmul)
+    uint32_t tcap = 4096;     // table slots per table buffer
+    uint32_t scap = 4096;     // staged output pairs per item
+    int threads = PROBE_THREADS;  // probe block size (one producer warp + consumers)
     int max_units[2] = {0, 0};
-    // where the build tables live; L2 tables follow one radix pass
-    int tables = VJ_TABLES_SHARED;
-    int fallbacks = 0;            // L2 plans that were redone with shared-memory tables
-    uint32_t l2_rc = 1u << 18;    // build rows per seq at most
-    uint32_t l2_region_slots = 0;
-    int l2_ring = 8;
-    int l2_lag = 2;
-    uint32_t l2_build_rows = 4096;
-    uint32_t l2_probe_rows = 8192;
-    uint32_t l2_outcap = 2048;
 };
 
 int ceil_log2(uint64_t x) {
@@ -62,59 +53,54 @@ int ceil_log2(uint64_t x) {
     return b;
 }
 
-// Shared memory a probe block may use: blocks of `threads` resident 1024 threads per SM
-// (two blocks of 512, four of 256, ...).
-size_t probe_smem_budget(const DeviceInfo &info, int threads) {
+// Shared memory the probe block may use (one block per SM), minus its static shared memory.
+size_t probe_smem_budget(const DeviceInfo &info) {
     const size_t per_block = info.smem_optin ? info.smem_optin : 48 * 1024;
-    const int blocks = threads >= 512 ? 2 : 1024 / threads;
-    const size_t share = (228 * 1024) / blocks - 2048;  // minus per-block reservations
-    return per_block < share ? per_block : share;
+    return per_block > 1024 ? per_block - 1024 : per_block;
 }
 
-// Build rows per partition the L2-table plan aims at: its table (8-byte slots, load
-// <= 1/3) and rows take a few MB of L2 each while a handful of partitions are in flight.
-constexpr uint64_t L2_PARTITION_ROWS = 1ull << 17;
+// Table slots per build row for a requested load (percent): 2, 4 or 8.
+uint32_t table_mul(int load_pct) {
+    if (load_pct <= 0) return 2;
+    uint32_t m = 2;
+    while (m < 8 && (int)(100 / m) > load_pct) m <<= 1;
+    return m;
+}
 
 template <int KW, int PB, int HS>
-Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt, int force_tables = -1) {
+Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_options *opt) {
+    using SMf = ProbeSmem<KW, PB, HS, true>;  // row-contiguous chunks are never smaller than columnar ones
+    using PT = typename Pair<PB>::T;
     Plan pl;
     if (opt && opt->probe_threads > 0) {
         int t = opt->probe_threads / 32 * 32;
         pl.threads = t < 64 ? 64 : (t > PROBE_THREADS ? PROBE_THREADS : t);
     }
-    const size_t budget = probe_smem_budget(info, pl.threads);
-    // largest table (then largest probe sub-chunk) whose probe block fits two per SM
-    bool found = false;
-    for (uint32_t sub = 1024; sub >= 256 && !found; sub >>= 1) {
-        for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
-            const uint32_t outcap = sub;
-            // sized for row-contiguous chunks, which are never smaller than columnar ones
-            if (ProbeSmem<KW, PB, HS, true>::bytes(rcap, 2 * rcap, sub, outcap) <= budget && (rcap >= 1024 || sub == 256)) {
-                pl.rcap = rcap;
-                pl.sub = sub;
-                pl.outcap = outcap;
-                found = true;
-                break;
-            }
+    pl.tmul = table_mul(opt ? opt->table_load_pct : 0);
+    const size_t budget = probe_smem_budget(info);
+    // largest build chunk (a power of two) whose buffers, tables and a stage of two pairs per
+    // build row fit one block
+    pl.rcap = 64;
+    for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
+        uint32_t tcap = 64;
+        while (tcap < rcap * pl.tmul) tcap <<= 1;
+        if (tcap <= 16384 && SMf::bytes(rcap, tcap, 2 * rcap) <= budget) {
+            pl.rcap = rcap;
+            break;
         }
     }
-    if (opt && opt->probe_sub_rows > 0) {
-        uint32_t sub = (uint32_t)opt->probe_sub_rows;
-        pl.sub = sub < 32 ? 32 : (sub > 2048 ? 2048 : sub);
-        pl.outcap = pl.sub;
-    }
     if (opt && opt->build_rows > 0) {
-        uint32_t want = 32;
+        uint32_t want = 64;
         while (want < (uint32_t)opt->build_rows && want < pl.rcap) want <<= 1;
         pl.rcap = want;
     }
-    if (opt && opt->probe_rows > 0) {
-        pl.schunk = (uint32_t)opt->probe_rows;
-        if (pl.sub > pl.schunk) {
-            pl.sub = pl.schunk < 32 ? 32 : pl.schunk;
-            pl.outcap = pl.sub;
-        }
-    }
+    pl.tcap = 64;
+    while (pl.tcap < pl.rcap * pl.tmul) pl.tcap <<= 1;
+    // the stage takes the rest of the block's shared memory
+    const size_t fixed = SMf::bytes(pl.rcap, pl.tcap, 0);
+    const size_t room = budget > fixed ? (budget - fixed) / (2 * sizeof(PT)) : 0;
+    pl.scap = (uint32_t)std::min<size_t>(room, 16384);
+    if (opt && opt->probe_rows > 0) pl.schunk = (uint32_t)std::max(32, opt->probe_rows);
     // passes / bits: the average build partition should fill about half a table
     int total_bits = 0;
     if (nr > pl.rcap) {
@@ -144,33 +130,6 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     }
     for (int p = 0; p < 2; p++) {
         if (pl.bits[p] > MAX_RADIX_BITS) pl.bits[p] = MAX_RADIX_BITS;
-    }
-    // Shared-memory tables unless the caller asks for L2 ones: on the 2^27 x 2^29 int64 join
-    // two passes + shared-memory tables take 23.4 ms, one pass + L2 tables 29 ms (builds by
-    // global CAS and lock-step cluster walks are latency-bound).
-    int tables = VJ_TABLES_SHARED;
-    if (opt && (opt->flags & VJ_JOIN_SHARED_TABLES)) tables = VJ_TABLES_SHARED;
-    if (opt && (opt->flags & VJ_JOIN_L2_TABLES)) tables = VJ_TABLES_L2;
-    if (force_tables >= 0) tables = force_tables;
-    if (tables == VJ_TABLES_L2 && nr > 0) {
-        pl.tables = VJ_TABLES_L2;
-        pl.passes = 1;
-        int b = ceil_log2((nr + L2_PARTITION_ROWS - 1) / L2_PARTITION_ROWS);
-        if (opt && (opt->flags & VJ_JOIN_FIXED_PASSES) && opt->radix_bits[0] > 0) b = opt->radix_bits[0];
-        pl.bits[0] = b < 1 ? 1 : (b > MAX_RADIX_BITS ? MAX_RADIX_BITS : b);
-        pl.bits[1] = 0;
-        // a seq holds at most twice the average partition (rounded to a power of two)
-        uint64_t avg = (nr + (1ull << pl.bits[0]) - 1) >> pl.bits[0];
-        uint32_t rc = 4096;
-        while (rc < 2 * avg && rc < (1u << 24)) rc <<= 1;
-        if (opt && opt->build_rows > 0) {  // smaller build chunks: several seqs per partition
-            uint32_t want = 64;
-            while (want < (uint32_t)opt->build_rows && want < rc) want <<= 1;
-            rc = want;
-        }
-        pl.l2_rc = rc;
-        pl.l2_region_slots = l2_cap(rc);
-        if (opt && opt->probe_rows > 0) pl.l2_probe_rows = opt->probe_rows < 32 ? 32u : (uint32_t)opt->probe_rows;
     }
     const int G0 = 2;
     const int G1 = 2 << pl.bits[0];
@@ -352,31 +311,14 @@ struct JoinRun {
     bool batch = false;
     uint32_t *batch_cnt = nullptr;
     uint32_t batch_parts = 1;
-    // L2-table build/probe (tables == VJ_TABLES_L2)
-    bool l2 = false;
-    L2Params l2p;
-    size_t l2_smem = 0;
-    int l2_grid = 0;
 };
-
-template <int KW, int PB, int HS>
-int l2_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
-    run->l2 = true;
-    run->l2_smem = (size_t)L2_WARPS * L2_WARP_STAGE * 2 * PB;
-    VJ_TRY(ensure_smem(l2_join_kernel<KW, PB, HS>, run->l2_smem));
-    int per_sm = 0;
-    VJ_TRY(blocks_per_sm(l2_join_kernel<KW, PB, HS>, L2_THREADS, run->l2_smem, &per_sm));
-    VJ_CHECK(per_sm >= 1, VJ_ERR_UNSUPPORTED, "L2-table probe kernel does not fit an SM");
-    run->l2_grid = per_sm * ctx->info.sms;  // all resident: the cooperative launch checks it
-    return VJ_OK;
-}
 
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
 int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     run->aos = AOS;
     run->batch = BATCH;
     run->threads = pl.threads;
-    run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, 2 * pl.rcap, pl.sub, pl.outcap);
+    run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, pl.tcap, pl.scap);
     VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS, BATCH>, run->probe_smem));
     return probe_grid<KW, PB, HS, AOS, BATCH>(ctx->info, pl.threads, run->probe_smem, &run->probe_grid);
 }
@@ -399,29 +341,13 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     }
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
-    const uint64_t item_cap = pl.tables == VJ_TABLES_L2 ? 0
-                              : batch                     ? 2ull * ((uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap) + 4096
-                                                          : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
+    const uint64_t item_cap = batch ? 2ull * ((uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap) + 4096 : (uint64_t)np + in.rows[1] / pl.schunk + in.rows[0] / pl.rcap + 4096;
     uint32_t *b_seg_begin = nullptr, *b_seg_end = nullptr, *b_cnt = nullptr;
     unsigned long long *plan_blocks = nullptr;
     uint16_t *bids[2] = {nullptr, nullptr};  // pass-2 buckets written by pass 1
     unsigned long long *b_out_begin = nullptr;
-    const bool l2 = pl.tables == VJ_TABLES_L2;
-    const uint32_t max_seqs = l2 ? (uint32_t)(np + in.rows[0] / pl.l2_rc + 1) : 0;
-    // work items when every partition is one seq (more are found by searching group offsets)
-    const uint64_t l2_items_est = l2 ? (uint64_t)in.rows[0] / pl.l2_build_rows + (uint64_t)in.rows[1] / pl.l2_probe_rows + 2ull * max_seqs + 4096 : 0;
-    const uint32_t l2_item_cap = (uint32_t)(l2_items_est < 0xffffffffull ? l2_items_est : 0xffffffffull);
-    L2Params Lq{};
+    uint32_t *item_join = nullptr;
     auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint4 **item_desc, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
-        if (l2) {
-            Lq.tables = c.take<unsigned long long>((size_t)pl.l2_ring * pl.l2_region_slots);
-            Lq.seq = c.take<uint4>(max_seqs);
-            Lq.group_start = c.take<uint32_t>((size_t)max_seqs + pl.l2_lag + 1);
-            Lq.built = c.take<uint32_t>(max_seqs);
-            Lq.probed = c.take<uint32_t>(max_seqs);
-            Lq.nseq = c.take<uint32_t>(4);
-            Lq.items = c.take<uint4>(l2_item_cap);
-        }
         for (int pass = 0; pass < 2; pass++) {
             for (int sd = 0; sd < 2; sd++) {
                 bufs[pass][sd] = pl.passes > pass ? c.take<char>((size_t)in.rows[sd] * L::STRIDE + 64) : nullptr;
@@ -439,6 +365,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         *item_begin = c.take<uint32_t>((size_t)np + 2);
         plan_blocks = c.take<unsigned long long>(((size_t)np + PLAN_BLOCK - 1) / PLAN_BLOCK);
         *item_desc = c.take<uint4>(item_cap);
+        item_join = batch ? c.take<uint32_t>(item_cap) : nullptr;
         *ticket = c.take<uint32_t>(1);
         *out_count = c.take<unsigned long long>(1);
         *error = c.take<uint32_t>(1);
@@ -534,12 +461,14 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.np = np;
     Pq.rcap = pl.rcap;
     Pq.schunk = pl.schunk;
-    Pq.outcap = pl.outcap;
-    Pq.sub_rows = pl.sub;
+    Pq.tcap = pl.tcap;
+    Pq.tmul = pl.tmul;
+    Pq.scap = pl.scap;
     // slot bits: the 14 bits right below the partition bits (tables hold at most 2^14 slots)
     Pq.slot_shift = 64 - (pl.bits[0] + pl.bits[1]) - 14;
     Pq.item_begin = item_begin;
     Pq.item_desc = item_desc;
+    Pq.item_join = item_join;
     Pq.item_cap = (uint32_t)(item_cap < 0xffffffffull ? item_cap : 0xffffffffull);
     Pq.ticket = ticket;
     Pq.out_count = out_count;
@@ -547,7 +476,6 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Pq.error = error;
     Pq.joins = (uint32_t)J;
     if (batch) {
-        Pq.s_join_begin = b_seg_begin + J;
         Pq.out_begin = b_out_begin;
         Pq.out_counts = in.counts;
         run->batch_cnt = b_cnt;
@@ -557,31 +485,6 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     run->plan_blocks = plan_blocks;
     run->d_out_count = out_count;
     run->d_error = error;
-    if (l2) {
-        Lq.r_rows = bufs[0][0];
-        Lq.s_rows = bufs[0][1];
-        Lq.r_begin = seg_begin;
-        Lq.r_end = seg_end;
-        Lq.s_begin = seg_begin + np;
-        Lq.s_end = seg_end + np;
-        Lq.np = np;
-        Lq.part_bits = pl.bits[0];
-        Lq.rc = pl.l2_rc;
-        Lq.build_rows = pl.l2_build_rows;
-        Lq.probe_rows = pl.l2_probe_rows;
-        Lq.ring = pl.l2_ring;
-        Lq.lag = pl.l2_lag;
-        Lq.region_slots = pl.l2_region_slots;
-        Lq.max_seqs = max_seqs;
-        Lq.item_cap = l2_item_cap;
-        Lq.ticket = ticket;
-        Lq.out_count = out_count;
-        Lq.outcap = pl.l2_outcap;
-        Lq.hs = hs;
-        Lq.error = error;
-        run->l2p = Lq;
-        return l2_setup<KW, PB, HS>(ctx, pl, run);
-    }
     if (pl.passes == 0) {
         return batch ? probe_setup<KW, PB, HS, false, true>(ctx, pl, run) : probe_setup<KW, PB, HS, false, false>(ctx, pl, run);
     }
@@ -591,21 +494,6 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
 template <int KW, int PB, int HS>
 int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
     profile_mark(ctx, PM_PROBE_BEGIN, stream);
-    if (run.l2) {
-        L2Params q = run.l2p;
-        q.out = run.probe.out;
-        q.capacity = run.probe.capacity;
-        // slots left by an earlier probe carry the tags this one reuses
-        VJ_CUDA(cudaMemsetAsync(q.tables, 0, (size_t)q.ring * q.region_slots * sizeof(unsigned long long), stream));
-        l2_plan_kernel<<<1, PLAN_THREADS, 0, stream>>>(q);
-        VJ_CUDA(cudaGetLastError());
-        // its blocks wait for one another's items: all must be resident
-        void *args[] = {&q};
-        VJ_CUDA(cudaLaunchCooperativeKernel((const void *)l2_join_kernel<KW, PB, HS>, dim3(run.l2_grid), dim3(L2_THREADS), args, run.l2_smem, stream));
-        profile_mark(ctx, PM_PROBE_END, stream);
-        ctx->launches += 2;
-        return VJ_OK;
-    }
     if (run.probe.out_begin) {
         const ProbeParams &Q = run.probe;
         batch_items_kernel<true><<<Q.joins, 256, 0, stream>>>(Q, run.batch_parts, run.batch_cnt, nullptr);
@@ -646,10 +534,10 @@ void finish_profile(vj_ctx *ctx, const Plan &pl, uint64_t nr, uint64_t ns, uint6
     p.kernel_launches = ctx->launches;
     p.radix_bits[0] = pl.bits[0];
     p.radix_bits[1] = pl.bits[1];
-    p.build_rows = pl.tables == VJ_TABLES_L2 ? pl.l2_rc : pl.rcap;
-    p.probe_rows = pl.tables == VJ_TABLES_L2 ? pl.l2_probe_rows : pl.schunk;
-    p.tables = pl.tables;
-    p.fallbacks = pl.fallbacks;
+    p.build_rows = pl.rcap;
+    p.probe_rows = pl.schunk;
+    p.tables = VJ_TABLES_SHARED;
+    p.fallbacks = 0;
     p.rows[0] = nr;
     p.rows[1] = ns;
     p.matches = matches;
@@ -718,14 +606,11 @@ int check_flags(uint32_t flags) {
     return VJ_OK;
 }
 
-// Plan, partition and probe once into (out, capacity); a plan with L2 tables that meets a
-// long duplicate cluster (error flag 8) is redone with shared-memory tables, whose
-// per-chunk tables bound the cost of duplicates. On return `run` holds the partitions of
-// the plan that succeeded (for a second probe into a larger buffer).
+// Plan, partition and probe once into (out, capacity). On return `run` holds the partitions
+// (for a second probe into a larger buffer).
 template <int KW, int PB, int HS>
-int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, int force_tables, void *out, uint64_t capacity, cudaStream_t stream, JoinRun *run, Plan *plan,
-               uint64_t *count) {
-    Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt, force_tables);
+int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, void *out, uint64_t capacity, cudaStream_t stream, JoinRun *run, Plan *plan, uint64_t *count) {
+    Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt);
     *run = JoinRun{};
     VJ_TRY((prepare<KW, PB, HS>(ctx, t, pl, hs, stream, run)));
     run->probe.out = out;
@@ -733,11 +618,6 @@ int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
     VJ_TRY((launch_probe<KW, PB, HS>(ctx, *run, stream)));
     uint32_t flags = 0;
     VJ_TRY(read_count(ctx, *run, stream, count, &flags));
-    if ((flags & 8u) && pl.tables == VJ_TABLES_L2) {
-        VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, VJ_TABLES_SHARED, out, capacity, stream, run, plan, count)));
-        plan->fallbacks += 1;
-        return VJ_OK;
-    }
     VJ_TRY(check_flags(flags));
     *plan = pl;
     return VJ_OK;
@@ -760,7 +640,7 @@ int join_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
     Plan pl;
     JoinRun run;
     uint64_t count = 0;
-    VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, -1, res->pairs, res->capacity, stream, &run, &pl, &count)));
+    VJ_TRY((probe_once<KW, PB, HS>(ctx, t, hs, opt, res->pairs, res->capacity, stream, &run, &pl, &count)));
     finish_profile(ctx, pl, t.rows[0], t.rows[1], count);
     if (count > res->capacity) {
         if (!res->owned) {
@@ -910,6 +790,11 @@ int dispatch(int kw, int pb, int hs, F &&f) {
     return set_error(VJ_ERR_UNSUPPORTED, "unsupported layout: key_words %d, payload_bytes %d, hash array bytes %d", kw, pb, hs);
 }
 
+int check_options(const vj_join_options *opt, const char *name) {
+    VJ_CHECK(!opt || !(opt->flags & VJ_JOIN_L2_TABLES), VJ_ERR_UNSUPPORTED, "%s: VJ_JOIN_L2_TABLES is no longer offered (shared-memory tables only)", name);
+    return VJ_OK;
+}
+
 HashSpec spec_from(const vj_join_options *opt, int mix) {
     HashSpec hs;
     hs.algo = opt && opt->hash_algo > 0 && opt->hash_algo < VJ_HASH_COUNT ? opt->hash_algo : VJ_HASH_FNV;
@@ -955,7 +840,7 @@ struct BuildProbeCall {
         Plan pl;
         JoinRun run;
         uint64_t n = 0;
-        VJ_TRY((probe_once<KW, PB, HS>(c.ctx, c.t, c.hs, c.opt, -1, rr.pairs, rr.capacity, c.stream, &run, &pl, &n)));
+        VJ_TRY((probe_once<KW, PB, HS>(c.ctx, c.t, c.hs, c.opt, rr.pairs, rr.capacity, c.stream, &run, &pl, &n)));
         finish_profile(c.ctx, pl, c.t.rows[0], c.t.rows[1], n);
         rr.count = n;
         return VJ_OK;
@@ -966,7 +851,7 @@ struct BuildProbeCall {
 // (the second pass's bookkeeping would grow with joins x buckets x buckets).
 template <int KW, int PB, int HS>
 int batch_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, uint64_t max_build_rows, void *pairs, uint32_t *d_status, cudaStream_t stream) {
-    Plan pl = make_plan<KW, PB, HS>(max_build_rows, 4 * max_build_rows, ctx->info, opt, VJ_TABLES_SHARED);
+    Plan pl = make_plan<KW, PB, HS>(max_build_rows, 4 * max_build_rows, ctx->info, opt);
     if (pl.passes == 2) {
         pl.passes = 1;
         pl.bits[0] = pl.bits[0] + pl.bits[1] > MAX_RADIX_BITS ? MAX_RADIX_BITS : pl.bits[0] + pl.bits[1];
@@ -1040,6 +925,7 @@ extern "C" int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, 
     VJ_TRY(check_table(r, "vj_join_batch: r"));
     VJ_TRY(check_table(s, "vj_join_batch: s"));
     VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: r and s must have the same key_words and payload_bytes");
+    VJ_TRY(check_options(options, "vj_join_batch"));
     // the pass's unit scan keeps one shared-memory word per unit, two units per join at least
     VJ_CHECK(joins >= 1 && joins <= 16384, VJ_ERR_UNSUPPORTED, "vj_join_batch: joins must be in [1, 16384] (got %u)", joins);
     VJ_CHECK(d_r_offsets && d_s_offsets && d_pair_offsets && d_counts, VJ_ERR_INVALID_ARGUMENT, "vj_join_batch: null offsets or counts");
@@ -1080,6 +966,7 @@ extern "C" int vj_join(vj_ctx *ctx, const vj_table *r, const vj_table *s, const 
     VJ_TRY(check_table(r, "vj_join: r"));
     VJ_TRY(check_table(s, "vj_join: s"));
     VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join: r and s must have the same key_words and payload_bytes");
+    VJ_TRY(check_options(options, "vj_join"));
     VJ_CUDA(cudaSetDevice(ctx->device));
     result->count = 0;
     if (!(result->pairs && result->capacity > 0)) {
@@ -1401,7 +1288,7 @@ struct ChunkJoinerT final : ChunkJoiner {
     }
 
     int build(cudaStream_t stream) override {
-        pl = make_plan<KW, PB, HS>(r.rows, s_rows, ctx->info, opt, VJ_TABLES_SHARED);
+        pl = make_plan<KW, PB, HS>(r.rows, s_rows, ctx->info, opt);
         if (pl.passes == 0) {
             direct = true;
             return VJ_OK;
@@ -1442,8 +1329,9 @@ struct ChunkJoinerT final : ChunkJoiner {
         Pq.np = np;
         Pq.rcap = pl.rcap;
         Pq.schunk = pl.schunk;
-        Pq.outcap = pl.outcap;
-        Pq.sub_rows = pl.sub;
+        Pq.tcap = pl.tcap;
+        Pq.tmul = pl.tmul;
+        Pq.scap = pl.scap;
         Pq.slot_shift = 64 - (pl.bits[0] + pl.bits[1]) - 14;
         Pq.item_begin = item_begin;
         Pq.item_desc = item_desc;
@@ -1631,6 +1519,7 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
     VJ_TRY(check_table(r, "vj_join_host: r"));
     VJ_TRY(check_table(s, "vj_join_host: s"));
     VJ_CHECK(r->key_words == s->key_words && r->payload_bytes == s->payload_bytes, VJ_ERR_INVALID_ARGUMENT, "vj_join_host: r and s must have the same layout");
+    VJ_TRY(check_options(options, "vj_join_host"));
     VJ_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = (cudaStream_t)stream;
     *count = 0;

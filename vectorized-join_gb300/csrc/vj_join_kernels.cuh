@@ -18,10 +18,9 @@
 //                buffered); each tile is ranked by bucket, sorted in shared memory and
 //                written out as one contiguous run per bucket
 // The probe stage plans (partition, build chunk, probe chunk) work items and runs a
-// persistent kernel that takes items from an atomic ticket, bulk-copies the build chunk
-// and builds an open-addressing table of its row indices in shared memory, then streams
-// the probe chunk through it in bulk-copied sub-chunks (double buffered), staging output
-// pairs in shared memory and writing them out in contiguous blocks.
+// persistent kernel in which one warp fetches items, copies their build rows in and
+// flushes their pairs out, while the other warps build shared-memory tables and probe
+// (see "probe kernel").
 #pragma once
 
 #include "vj_internal.cuh"
@@ -30,7 +29,6 @@ namespace vj {
 
 constexpr int MAX_RADIX_BITS = 12;
 constexpr int PART_THREADS = 512;
-constexpr int PROBE_THREADS = 512;
 constexpr int PLAN_THREADS = 1024;
 
 struct HashSpec {
@@ -101,13 +99,15 @@ struct ProbeParams {
     const uint32_t *s_begin, *s_end;
     uint32_t r_rows, s_rows;
     int np;
-    uint32_t rcap;         // build rows per item (a power of two; table capacity <= 2*rcap)
+    uint32_t rcap;         // build rows per item (a power of two)
     uint32_t schunk;       // probe rows per item
-    uint32_t outcap;       // staged output pairs per block
+    uint32_t tcap;         // table slots per table buffer (a power of two, >= rcap * tmul)
+    uint32_t tmul;         // table slots per build row of an item (2, 4 or 8: load <= 1/tmul)
+    uint32_t scap;         // staged output pairs per item
     uint32_t *item_begin;  // [np+2]: prefix, total, and whether item_desc is filled
     uint4 *item_desc;      // [item_cap]: build rows [x, y), probe rows [z, w) of each item
+    uint32_t *item_join;   // [item_cap]: join of each item (batches of joins)
     uint32_t item_cap;
-    uint32_t sub_rows;     // probe rows per bulk copy
     int slot_shift;        // table slot = (mix_hash(hash) >> slot_shift) & (capacity - 1)
     uint32_t *ticket;
     unsigned long long *out_count;
@@ -115,10 +115,9 @@ struct ProbeParams {
     uint64_t capacity;
     HashSpec hs;
     uint32_t *error;
-    // batches of joins (out_begin set): join j's probe rows start at s_join_begin[j]; its
-    // pairs go to out[out_begin[j], out_begin[j+1]), counted in out_counts[j]
+    // batches of joins (out_begin set): join j's pairs go to out[out_begin[j],
+    // out_begin[j+1]), counted in out_counts[j]; item_join gives each item's join
     uint32_t joins;
-    const uint32_t *s_join_begin;
     const unsigned long long *out_begin;
     unsigned long long *out_counts;
 };
@@ -764,18 +763,6 @@ __device__ __forceinline__ void out_range(const QP &Q, uint32_t j, unsigned long
     }
 }
 
-// Join of a work item whose probe rows start at s0: the last join starting at or before it.
-__device__ __forceinline__ uint32_t join_of(const ProbeParams &Q, uint32_t s0) {
-    if (!Q.out_begin) return 0;
-    uint32_t lo = 0, hi = Q.joins - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (Q.s_join_begin[mid] <= s0) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // ---- work items of a batch of joins
 //
 // Join j's build and probe rows after the pass are `parts` adjacent partitions on each side
@@ -825,7 +812,10 @@ __global__ void __launch_bounds__(256) batch_items_kernel(ProbeParams Q, uint32_
             uint32_t k = run + excl;
             for (uint32_t r0 = d.x; r0 < d.y; r0 += Q.rcap) {
                 for (uint32_t s0 = d.z; s0 < d.w; s0 += Q.schunk) {
-                    if (k < Q.item_cap) Q.item_desc[k] = make_uint4(r0, min(d.y, r0 + Q.rcap), s0, min(d.w, s0 + Q.schunk));
+                    if (k < Q.item_cap) {
+                        Q.item_desc[k] = make_uint4(r0, min(d.y, r0 + Q.rcap), s0, min(d.w, s0 + Q.schunk));
+                        Q.item_join[k] = j;
+                    }
                     k++;
                 }
             }
@@ -875,16 +865,81 @@ struct Pair<8> {
     static __device__ __forceinline__ T make(unsigned long long a, unsigned long long b) { return make_ulonglong2(a, b); }
 };
 
-// Shared memory of the probe kernel: barriers, the build chunk as copied, the table of
-// build-row indices (16-bit), two probe sub-chunks and two output staging buffers of
-// `outcap` pairs.
-template <int KW, int PB, int HS, bool AOS>
-struct ProbeSmem {
-    using C = Chunk<KW, PB, HS, AOS>;
-    __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t sub, uint32_t outcap) {
-        return 32 + C::bytes(rcap) + ((size_t)tcap * 2 + 15) / 16 * 16 + 2 * C::bytes(sub) + 2 * (size_t)outcap * 2 * PB;
-    }
+// ------------------------------------------------------------------ probe kernel
+//
+// Persistent, one block per SM: PROBE_THREADS - 32 "consumer" threads build and probe, the
+// last warp ("producer") runs up to two work items ahead of them and never probes.
+//
+//   producer, item k (buffer b = k & 1):
+//     wait empty[b] (the consumers are done with item k - 2)
+//     bulk-copy item k's build rows into rbuf[b]            (full[b]: arrival 1 + bytes)
+//     flush item k - 2's staged pairs: one atomic on the output counter, one bulk store
+//     publish item k's descriptor, clear its pair count     (full[b]: arrival 2)
+//     claim item k + 1 by ticket, L2-prefetch its build and probe rows
+//   consumers, item k:
+//     wait full[b]; load their first probe rows into registers (in flight during the build)
+//     insert the build rows into table[b] (u32 slots: tag << 16 | row + 1, atomicCAS)
+//     named barrier over the consumers: the table is complete (the only block-level wait)
+//     probe: rows straight from global memory, J per thread per round, matches staged per
+//     item in stage[b] (one shared-memory reservation per warp and round)
+//     arrive empty[b]
+//
+// Tables are never cleared: a slot belongs to the current item when its tag equals the
+// item's tag (the use count of the table buffer), so stale slots read as empty. Staged pairs
+// leave with one bulk store per item in the order of an atomic reservation; pairs past the
+// stage's capacity (only when an item has more matches than it holds) are written directly
+// with a per-warp reservation.
+
+constexpr int PROBE_THREADS = 1024;
+constexpr int PROBE_J = 4;  // probe rows per consumer thread per round
+
+template <int KW, int PB, int HS>
+struct ProbeRow {
+    Key<KW> key;
+    typename PayloadType<PB>::T pay;
+    uint64_t hash;
 };
+
+// Probe row s, straight from global memory (read once: streaming loads).
+template <int KW, int PB, int HS, bool AOS>
+__device__ __forceinline__ void load_probe_row(const ProbeParams &Q, uint32_t s, ProbeRow<KW, PB, HS> &r) {
+    using L = Layout<KW, PB, HS>;
+    using Pt = typename PayloadType<PB>::T;
+    if (AOS) {
+        const unsigned char *p = (const unsigned char *)Q.s_rows_in + (size_t)s * L::STRIDE;
+        uint32_t w[L::STRIDE / 4];
+        if (L::STRIDE % 16 == 0) {
+#pragma unroll
+            for (int o = 0; o < L::STRIDE / 16; o++) {
+                const uint4 v = __ldcs((const uint4 *)p + o);
+                w[4 * o] = v.x;
+                w[4 * o + 1] = v.y;
+                w[4 * o + 2] = v.z;
+                w[4 * o + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < L::STRIDE / 8; o++) {
+                const uint2 v = __ldcs((const uint2 *)p + o);
+                w[2 * o] = v.x;
+                w[2 * o + 1] = v.y;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < KW; i++) r.key.w[i] = w[i];
+        if (PB == 8) r.pay = (Pt)(((unsigned long long)w[L::PAY_OFF / 4 + 1] << 32) | w[L::PAY_OFF / 4]);
+        else r.pay = (Pt)w[L::PAY_OFF / 4];
+        if (HS == 8) r.hash = ((uint64_t)w[L::HASH_OFF / 4 + 1] << 32) | w[L::HASH_OFF / 4];
+        else if (HS == 4) r.hash = w[L::HASH_OFF / 4];
+        else r.hash = 0;
+    } else {
+        r.key = load_key_stream<KW>(Q.s_keys, s);
+        r.pay = __ldcs((const Pt *)Q.s_pay + s);
+        if (HS == 8) r.hash = __ldcs((const unsigned long long *)Q.s_hash + s);
+        else if (HS == 4) r.hash = __ldcs((const uint32_t *)Q.s_hash + s);
+        else r.hash = 0;
+    }
+}
 
 // Rows of work item `it`: build rows [x, y), probe rows [z, w) -- from the planner's
 // descriptor, or (plans too large for the descriptor array) from a search of the prefix.
@@ -906,327 +961,343 @@ __device__ __forceinline__ uint4 item_rows(const ProbeParams &Q, uint32_t it, bo
     return make_uint4(r0, min(re, r0 + Q.rcap), s0, min(se, s0 + Q.schunk));
 }
 
-// End of a probe sub-chunk (all threads): reserve the output range of the buffer just
-// filled (one atomic, whose result is read one sub-chunk later), copy out the buffer
-// filled before it, and switch buffers. The atomic's latency overlaps a sub-chunk of work.
-template <int PB, bool BATCH, typename QP>
-__device__ __forceinline__ void rotate_stage(const QP &Q, typename Pair<PB>::T *stage0, uint32_t &cur, uint32_t *out_n, uint32_t *flush_n, unsigned long long *flush_base, uint32_t *pend_n,
-                                             unsigned long long *pend_base, uint32_t join, uint32_t *pend_join, uint32_t *flush_join) {
+// Shared memory of the probe kernel (dynamic part): barriers, two build-row buffers, two
+// tables, two output stages.
+template <int KW, int PB, int HS, bool AOS>
+struct ProbeSmem {
+    using C = Chunk<KW, PB, HS, AOS>;
     using PT = typename Pair<PB>::T;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        *flush_base = *pend_base;
-        *flush_n = *pend_n;
-        if constexpr (BATCH) *flush_join = *pend_join;
-        const uint32_t n = min(*out_n, Q.outcap);
-        *pend_n = n;
-        if constexpr (BATCH) *pend_join = join;
-        if (n) *pend_base = atomicAdd(out_counter<BATCH>(Q, join), (unsigned long long)n);
-        *out_n = 0;
+    __host__ __device__ static size_t rbuf_bytes(uint32_t rcap) { return (C::bytes(rcap) + 127) / 128 * 128; }
+    __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t scap) {
+        return 128 + 2 * rbuf_bytes(rcap) + 2 * (size_t)tcap * 4 + 2 * (size_t)scap * sizeof(PT);
     }
-    __syncthreads();
-    const uint32_t n = *flush_n;
-    unsigned long long first, cap;
-    out_range<BATCH>(Q, BATCH ? *flush_join : 0u, &first, &cap);
-    const unsigned long long base = *flush_base;
-    const PT *src = stage0 + (size_t)(cur ^ 1) * Q.outcap;
-    PT *out = (PT *)Q.out + first;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        if (base + i < cap) __stcs(out + base + i, src[i]);
+};
+
+// Pairs of one warp's group of matches: lanes with `want` write `pair` at stage positions
+// pos0 + (rank among the group); positions past the stage go straight to the output with
+// their own reservation.
+template <int PB, bool BATCH>
+__device__ __forceinline__ void stage_pairs(const ProbeParams &Q, typename Pair<PB>::T *stage, uint32_t pos, bool want, const typename Pair<PB>::T &pair, uint32_t join, unsigned long long o_first,
+                                            unsigned long long o_cap) {
+    using PT = typename Pair<PB>::T;
+    const bool over = want && pos >= Q.scap;
+    const uint32_t ob = __ballot_sync(0xffffffffu, over);
+    if (ob) {
+        const int leader = __ffs(ob) - 1;
+        unsigned long long g0 = 0;
+        if ((int)(threadIdx.x & 31) == leader) g0 = atomicAdd(out_counter<BATCH>(Q, join), (unsigned long long)__popc(ob));
+        g0 = __shfl_sync(0xffffffffu, g0, leader);
+        if (over) {
+            const unsigned long long g = g0 + __popc(ob & lanemask_lt());
+            if (g < o_cap) ((PT *)Q.out)[o_first + g] = pair;
+        }
     }
-    cur ^= 1;
+    if (want && !over) stage[pos] = pair;
 }
 
-// BATCH: a batch of joins, each item's pairs go to its join's output range.
+// Producer: the n_staged pairs an item of join `join` staged in `stage` go to the output
+// behind one reservation on the join's counter. Whole warp; n_staged and join are lane 0's
+// values, the other lanes take them from it.
+template <int PB, bool BATCH>
+__device__ __forceinline__ void flush_stage(const ProbeParams &Q, const typename Pair<PB>::T *stage, uint32_t n_staged, uint32_t join) {
+    using PT = typename Pair<PB>::T;
+    const uint32_t lane = threadIdx.x & 31;
+    join = __shfl_sync(0xffffffffu, join, 0);
+    const uint32_t n = min(__shfl_sync(0xffffffffu, n_staged, 0), Q.scap);
+    if (n == 0) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(out_counter<BATCH>(Q, join), (unsigned long long)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    unsigned long long first, cap;
+    out_range<BATCH>(Q, join, &first, &cap);
+    if (base >= cap) return;
+    const uint32_t m = (uint32_t)min((unsigned long long)n, cap - base);
+    PT *dst = (PT *)Q.out + first + base;
+    if (sizeof(PT) == 16 && ((uintptr_t)dst & 15) == 0) {
+        if (lane == 0) {
+            bulk_s2g(dst, stage, m * 16u);
+            bulk_commit();
+            bulk_wait_read();
+        }
+    } else {
+        for (uint32_t i = lane; i < m; i += 32) __stcs(dst + i, stage[i]);
+    }
+    __syncwarp();
+}
+
+// BATCH: a batch of joins; each item's pairs go to its join's output range.
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
-__global__ void __launch_bounds__(PROBE_THREADS) probe_kernel(ProbeParams Q) {
+__global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) {
     using C = Chunk<KW, PB, HS, AOS>;
     using Pt = typename PayloadType<PB>::T;
     using PT = typename Pair<PB>::T;
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    const uint32_t tcap_max = 2 * Q.rcap;  // rcap is a power of two
-    // layout: barriers | build chunk | table | probe sub-chunks x2 | output staging x2
-    uint64_t *bar = (uint64_t *)s_raw;  // [0] build chunk, [1], [2] probe sub-chunks
-    unsigned char *rbuf = s_raw + 32;
-    uint16_t *t_idx = (uint16_t *)(rbuf + C::bytes(Q.rcap));  // build row + 1, 0 = empty
-    unsigned char *sbuf0 = (unsigned char *)t_idx + ((size_t)tcap_max * 2 + 15) / 16 * 16;
-    const size_t sbytes = C::bytes(Q.sub_rows);
-    PT *stage0 = (PT *)(sbuf0 + 2 * sbytes);
+    using SM = ProbeSmem<KW, PB, HS, AOS>;
+    using Row = ProbeRow<KW, PB, HS>;
+    constexpr int J = PROBE_J;
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    uint64_t *full = (uint64_t *)s_raw;  // [2]: build rows landed + descriptor published
+    uint64_t *empty = full + 2;          // [2]: consumers done with the item
+    const size_t rbytes = SM::rbuf_bytes(Q.rcap);
+    unsigned char *rbuf0 = s_raw + 128;
+    uint32_t *tab0 = (uint32_t *)(rbuf0 + 2 * rbytes);
+    PT *stage0 = (PT *)(tab0 + 2 * (size_t)Q.tcap);
+    __shared__ uint4 s_desc[2];
+    __shared__ uint32_t s_item[2], s_join[2], s_dups[2], s_out_n[2];
+    __shared__ uint32_t s_rdelta[2][3];
 
-    __shared__ uint32_t s_item, s_next_item;
-    __shared__ uint4 s_rows, s_next_rows;
-    __shared__ uint32_t s_join, s_next_join;    // batches of joins: the item's join
-    __shared__ uint32_t s_pend_join, s_flush_join;
-    __shared__ uint32_t s_out_n;                 // pairs staged in the current buffer
-    __shared__ uint32_t s_flush_n;               // pairs of the other buffer awaiting copy-out
-    __shared__ unsigned long long s_flush_base;  // their output position
-    __shared__ uint32_t s_rdelta[3];
-    __shared__ uint32_t s_sdelta[2][3];
-    __shared__ int s_dups;
-    const int lane = threadIdx.x & 31;
-    const uint32_t total_items = Q.item_begin[Q.np];
+    const uint32_t NC = blockDim.x - 32;  // consumer threads (a multiple of 32)
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t total = Q.item_begin[Q.np];
     const bool direct = Q.item_begin[Q.np + 1] != 0;
-    // Output: sub-chunk k stages into buffer k & 1. At its end thread 0 reserves its output
-    // range with one atomic, whose result is only read at the end of sub-chunk k + 1, when
-    // the buffer is copied out -- the atomic's latency overlaps a sub-chunk of probing.
-    __shared__ unsigned long long s_pend_base;  // reservation of the buffer not yet copied
-    __shared__ uint32_t s_pend_n;
-    uint32_t cur = 0;                           // staging buffer being filled (uniform)
+
     if (threadIdx.x == 0) {
-        s_out_n = 0;
-        s_flush_n = 0;
-        s_pend_base = 0;
-        s_pend_n = 0;
-        s_pend_join = 0;
-        s_flush_join = 0;
-        s_next_join = 0;
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        mbar_init(&bar[2], 1);
+        mbar_init(&full[0], 2);
+        mbar_init(&full[1], 2);
+        mbar_init(&empty[0], NC / 32);
+        mbar_init(&empty[1], NC / 32);
+        s_out_n[0] = s_out_n[1] = 0;
+        s_dups[0] = s_dups[1] = 0;
         fence_proxy_async();
-        s_next_item = atomicAdd(Q.ticket, 1u);
-        if (s_next_item < total_items) {
-            const uint4 d = item_rows(Q, s_next_item, direct);
-            s_next_rows = d;
-            if constexpr (BATCH) s_next_join = join_of(Q, d.z);
-            C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d.x, d.y);
-            C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d.z, d.w);
-        }
     }
-    uint32_t r_loads = 0;   // build-chunk copies waited for so far (parity of bar[0])
-    uint32_t s_issued = 0;  // probe sub-chunk copies issued / waited for
-    uint32_t s_waited = 0;
+    for (uint32_t i = threadIdx.x; i < 2 * Q.tcap; i += blockDim.x) tab0[i] = 0;
+    __syncthreads();
 
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            s_item = s_next_item;
-            s_rows = s_next_rows;
-            s_join = s_next_join;
-            s_dups = 0;
-        }
-        __syncthreads();
-        const uint32_t item = s_item;
-        if (item >= total_items) break;
-        if (threadIdx.x == 32) {
-            // claim the next item and start its rows towards L2; its latency overlaps this
-            // item's build-chunk copy (thread 0 drives the copies)
-            const uint32_t nx = atomicAdd(Q.ticket, 1u);
-            s_next_item = nx;
-            if (nx < total_items) {
-                const uint4 dn = item_rows(Q, nx, direct);
-                s_next_rows = dn;
-                if constexpr (BATCH) s_next_join = join_of(Q, dn.z);
-                C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, dn.x, dn.y);
-                C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, dn.z, dn.w);
+    if (warp == NC / 32) {
+        // ---------------------------------------------------------------- producer warp
+        const bool l0 = lane == 0;
+        uint32_t t_cur = 0, t_nxt = 0, j_cur = 0;
+        uint4 d_cur = make_uint4(0, 0, 0, 0);
+        if (l0) {
+            t_cur = atomicAdd(Q.ticket, 1u);
+            if (t_cur < total) {
+                d_cur = item_rows(Q, t_cur, direct);
+                if constexpr (BATCH) j_cur = Q.item_join[t_cur];
+                C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d_cur.z, d_cur.w);
             }
+            t_nxt = atomicAdd(Q.ticket, 1u);
         }
-        const uint4 d = s_rows;
-        const uint32_t r0 = d.x, r1 = d.y, s0 = d.z, s1 = d.w;
-        const uint32_t join = BATCH ? s_join : 0u;
-        unsigned long long o_first, o_cap;  // this item's output range (overflow writes)
-        out_range<BATCH>(Q, join, &o_first, &o_cap);
-        const uint32_t nr = r1 - r0;
-        const uint32_t nsub = (s1 - s0 + Q.sub_rows - 1) / Q.sub_rows;
-        uint32_t cap = 64;
-        while (cap < 4 * nr && cap < tcap_max) cap <<= 1;
-        const uint32_t cmask = cap - 1;
-
-        if (threadIdx.x == 0) {
-            fence_proxy_async();
-            C::issue(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, r0, r1, Q.rcap, rbuf, &bar[0], s_rdelta);
-            const uint32_t sbi = s_issued & 1;
-            C::issue(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, s0, min(s1, s0 + Q.sub_rows), Q.sub_rows, sbuf0 + sbi * sbytes, &bar[1 + sbi], s_sdelta[sbi]);
-        }
-        s_issued++;
-        for (uint32_t i = threadIdx.x; i < cap / 8; i += blockDim.x) ((uint4 *)t_idx)[i] = make_uint4(0, 0, 0, 0);
-        const bool ok_r = block_wait(&bar[0], r_loads & 1);
-        r_loads++;
-        if (!ok_r) {
-            if (threadIdx.x == 0) {
-                atomicOr(Q.error, 4u);
-                mbar_wait(&bar[1 + ((s_issued - 1) & 1)], ((s_issued - 1) >> 1) & 1);
-            }
-            return;
-        }
-        // ---- build: table of build-row indices (+1) keyed by the mixed hash; an equal key
-        // met on the way marks the chunk as having duplicate keys
-        const C R = C::view(rbuf, Q.rcap, s_rdelta);
-        for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) {
-            const Key<KW> key = R.key(i);
-            const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
-            uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
-            uint32_t tries = 0;
-            bool dup = false;
-            for (;;) {
-                const uint32_t prev = atomicCAS(&t_idx[slot], (unsigned short)0, (unsigned short)(i + 1));
-                if (prev == 0u) break;
-                dup |= key_equal<KW>(R.key(prev - 1), key);
-                slot = (slot + 1) & cmask;
-                if (++tries > cap) {  // cannot happen: at most half the slots are used
-                    atomicOr(Q.error, 1u);
+        uint32_t k = 0;
+        bool ok = true;
+        for (;; k++) {
+            const uint32_t b = k & 1;
+            if (k >= 2) {
+                bool w = true;
+                if (l0) w = mbar_wait(&empty[b], ((k - 2) >> 1) & 1);
+                __syncwarp();  // the other lanes read the stage after lane 0's wait
+                if (!__shfl_sync(0xffffffffu, (uint32_t)w, 0)) {
+                    ok = false;
                     break;
                 }
             }
-            if (dup) s_dups = 1;
-        }
-        __syncthreads();
-        const bool dups = s_dups != 0;
-
-        // ---- probe the sub-chunks of this item, the next one loading meanwhile
-        for (uint32_t sub = 0; sub < nsub; sub++) {
-            const uint32_t sbi = s_waited & 1;
-            const bool ok = block_wait(&bar[1 + sbi], (s_waited >> 1) & 1);
-            s_waited++;
-            if (!ok) {
-                if (threadIdx.x == 0) atomicOr(Q.error, 4u);
-                return;
-            }
-            if (sub + 1 < nsub) {
-                if (threadIdx.x == 0) {
+            const bool valid = __shfl_sync(0xffffffffu, (uint32_t)(t_cur < total), 0) != 0;
+            if (l0) {
+                if (valid) {
                     fence_proxy_async();
-                    const uint32_t a = s0 + (sub + 1) * Q.sub_rows;
-                    const uint32_t nbi = s_issued & 1;
-                    C::issue(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, a, min(s1, a + Q.sub_rows), Q.sub_rows, sbuf0 + nbi * sbytes, &bar[1 + nbi], s_sdelta[nbi]);
+                    C::issue(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d_cur.x, d_cur.y, Q.rcap, rbuf0 + b * rbytes, &full[b], s_rdelta[b]);
+                } else {
+                    mbar_arrive(&full[b]);
                 }
-                s_issued++;
             }
-            const C Sv = C::view(sbuf0 + sbi * sbytes, Q.sub_rows, s_sdelta[sbi]);
-            PT *stage = stage0 + (size_t)cur * Q.outcap;
-            const uint32_t a = s0 + sub * Q.sub_rows;
-            const uint32_t ns = min(s1 - a, Q.sub_rows);
+            if (k >= 2) flush_stage<PB, BATCH>(Q, stage0 + (size_t)b * Q.scap, s_out_n[b], s_join[b]);
+            if (l0) {
+                s_item[b] = t_cur;
+                s_desc[b] = d_cur;
+                s_join[b] = j_cur;
+                s_out_n[b] = 0;
+                mbar_arrive(&full[b]);
+            }
+            if (!valid) break;
+            if (l0) {
+                t_cur = t_nxt;
+                if (t_cur < total) {
+                    d_cur = item_rows(Q, t_cur, direct);
+                    if constexpr (BATCH) j_cur = Q.item_join[t_cur];
+                    C::prefetch(Q.r_keys, Q.r_pay, Q.r_hash, Q.r_rows_in, d_cur.x, d_cur.y);
+                    C::prefetch(Q.s_keys, Q.s_pay, Q.s_hash, Q.s_rows_in, d_cur.z, d_cur.w);
+                }
+                t_nxt = atomicAdd(Q.ticket, 1u);
+            }
+        }
+        if (ok && k >= 1) {
+            // the item before the end mark: its pairs are still staged
+            const uint32_t b = (k - 1) & 1;
+            bool w = true;
+            if (l0) w = mbar_wait(&empty[b], ((k - 1) >> 1) & 1);
+            __syncwarp();
+            if (__shfl_sync(0xffffffffu, (uint32_t)w, 0)) flush_stage<PB, BATCH>(Q, stage0 + (size_t)b * Q.scap, s_out_n[b], s_join[b]);
+            else ok = false;
+        }
+        if (l0) {
+            if (!ok) atomicOr(Q.error, 4u);
+            bulk_wait_all();
+        }
+        return;
+    }
+
+    // -------------------------------------------------------------------- consumer warps
+    const uint32_t c = threadIdx.x;
+    Row rows[J];
+    for (uint32_t k = 0;; k++) {
+        const uint32_t b = k & 1;
+        const bool got = mbar_wait(&full[b], (k >> 1) & 1);
+        const uint32_t item = got ? s_item[b] : 0xffffffffu;
+        const bool stop = !got || item >= total;
+        const uint32_t use = k >> 1;                  // uses of table b before this one
+        const uint32_t tag = use % 65535u + 1u;       // 1..65535
+        uint32_t *T = tab0 + (size_t)b * Q.tcap;
+        if (use > 0 && use % 65535u == 0) {
+            // the tag wraps: clear the table (its last item finished before the previous
+            // item's table barrier)
+            for (uint32_t i = c; i < Q.tcap; i += NC) T[i] = 0;
+            bar_sync(1, NC);
+        }
+        uint4 d = make_uint4(0, 0, 0, 0);
+        uint32_t join = 0;
+        if (!stop) {
+            d = s_desc[b];
+            if constexpr (BATCH) join = s_join[b];
+        }
+        const uint32_t nr = d.y - d.x, ns = d.w - d.z;
+        // first round of probe rows: their loads overlap the build
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const uint32_t i = c + (uint32_t)j * NC;
+            if (i < ns) load_probe_row<KW, PB, HS, AOS>(Q, d.z + i, rows[j]);
+        }
+        uint32_t cap = 64;
+        while (cap < nr * Q.tmul && cap < Q.tcap) cap <<= 1;
+        const uint32_t cmask = cap - 1;
+        const C R = C::view(rbuf0 + b * rbytes, Q.rcap, s_rdelta[b]);
+        // ---- build: slot = tag << 16 | (row + 1); an equal key met on the way marks the item
+        // as having duplicate build keys
+        bool dup = false;
+        for (uint32_t i = c; i < nr; i += NC) {
+            const Key<KW> key = R.key(i);
+            const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
+            uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
+            const uint32_t val = (tag << 16) | (i + 1);
+            uint32_t cur = T[slot];
+            for (uint32_t tries = 0;;) {
+                if ((cur >> 16) != tag) {
+                    const uint32_t prev = atomicCAS(&T[slot], cur, val);
+                    if (prev == cur) break;
+                    cur = prev;
+                    continue;
+                }
+                dup |= key_equal<KW>(R.key((cur & 0xffffu) - 1), key);
+                if (++tries > cap) {  // cannot happen: at most 1/tmul of the slots are used
+                    atomicOr(Q.error, 1u);
+                    break;
+                }
+                slot = (slot + 1) & cmask;
+                cur = T[slot];
+            }
+        }
+        if (dup) s_dups[b] = tag;
+        if (bar_or(1, NC, stop)) {
+            if (!got) atomicOr(Q.error, 4u);
+            break;
+        }
+        const bool dups = s_dups[b] == tag;
+        unsigned long long o_first, o_cap;  // this item's output range (direct writes)
+        out_range<BATCH>(Q, join, &o_first, &o_cap);
+        PT *stage = stage0 + (size_t)b * Q.scap;
+        const uint32_t lt = lanemask_lt();
+
+        for (uint32_t r0 = 0; r0 < ns; r0 += J * NC) {
+            if (r0 > 0) {
+#pragma unroll
+                for (int j = 0; j < J; j++) {
+                    const uint32_t i = r0 + c + (uint32_t)j * NC;
+                    if (i < ns) load_probe_row<KW, PB, HS, AOS>(Q, d.z + i, rows[j]);
+                }
+            }
             if (!dups) {
-                // Unique build keys: a probe row has at most one match. Each thread resolves
-                // two rows on its own, then the warp emits its matches with one reservation.
-                for (uint32_t base = 0; base < ns; base += 2 * blockDim.x) {
-                    const uint32_t i0 = base + threadIdx.x, i1 = i0 + blockDim.x;
-                    bool a0 = i0 < ns, a1 = i1 < ns;
-                    Key<KW> k0, k1;
-                    uint64_t h0 = 0, h1 = 0;
-                    uint32_t sl0 = 0, sl1 = 0;
-                    if (a0) {
-                        k0 = Sv.key(i0);
-                        h0 = HS ? Sv.hash(i0) : row_hash<KW>(k0, Q.hs);
-                        sl0 = (uint32_t)(mix_hash(h0) >> Q.slot_shift) & cmask;
-                    }
-                    if (a1) {
-                        k1 = Sv.key(i1);
-                        h1 = HS ? Sv.hash(i1) : row_hash<KW>(k1, Q.hs);
-                        sl1 = (uint32_t)(mix_hash(h1) >> Q.slot_shift) & cmask;
-                    }
-                    int m0 = -1, m1 = -1;
-                    while (a0 | a1) {
-                        if (a0) {
-                            const uint32_t e = t_idx[sl0];
-                            if (e == 0) {
-                                a0 = false;
-                            } else if (key_equal<KW>(R.key(e - 1), k0) && (!HS || R.hash(e - 1) == h0)) {
-                                m0 = (int)e - 1;
-                                a0 = false;
-                            } else {
-                                sl0 = (sl0 + 1) & cmask;
+                // Unique build keys: a probe row matches at most one build row. Every lane
+                // resolves its J rows, then the warp stages all its matches behind one
+                // shared-memory reservation.
+                int m[J];
+                uint32_t bal[J];
+                uint32_t cnt = 0;
+#pragma unroll
+                for (int j = 0; j < J; j++) {
+                    m[j] = -1;
+                    if (r0 + c + (uint32_t)j * NC < ns) {
+                        const uint64_t h = HS ? rows[j].hash : row_hash<KW>(rows[j].key, Q.hs);
+                        uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
+                        for (uint32_t t = 0; t < cap; t++) {
+                            const uint32_t e = T[slot];
+                            if ((e >> 16) != tag) break;
+                            const uint32_t bi = (e & 0xffffu) - 1;
+                            if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == h)) {
+                                m[j] = (int)bi;
+                                break;
                             }
-                        }
-                        if (a1) {
-                            const uint32_t e = t_idx[sl1];
-                            if (e == 0) {
-                                a1 = false;
-                            } else if (key_equal<KW>(R.key(e - 1), k1) && (!HS || R.hash(e - 1) == h1)) {
-                                m1 = (int)e - 1;
-                                a1 = false;
-                            } else {
-                                sl1 = (sl1 + 1) & cmask;
-                            }
+                            slot = (slot + 1) & cmask;
                         }
                     }
-                    const uint32_t b0 = __ballot_sync(0xffffffffu, m0 >= 0);
-                    const uint32_t b1 = __ballot_sync(0xffffffffu, m1 >= 0);
-                    const uint32_t total = __popc(b0) + __popc(b1);
-                    if (total) {
-                        uint32_t pos0 = 0;
-                        if (lane == 0) pos0 = atomicAdd(&s_out_n, total);
-                        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-                        const uint32_t lt = lanemask_lt();
-                        if (m0 >= 0) {
-                            const uint32_t pos = pos0 + __popc(b0 & lt);
-                            const PT pr = Pair<PB>::make(R.pay((uint32_t)m0), Sv.pay(i0));
-                            if (pos < Q.outcap) {
-                                stage[pos] = pr;
-                            } else {
-                                const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
-                                if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
-                            }
-                        }
-                        if (m1 >= 0) {
-                            const uint32_t pos = pos0 + __popc(b0) + __popc(b1 & lt);
-                            const PT pr = Pair<PB>::make(R.pay((uint32_t)m1), Sv.pay(i1));
-                            if (pos < Q.outcap) {
-                                stage[pos] = pr;
-                            } else {
-                                const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
-                                if (g < o_cap) ((PT *)Q.out)[o_first + g] = pr;
-                            }
+                    bal[j] = __ballot_sync(0xffffffffu, m[j] >= 0);
+                    cnt += __popc(bal[j]);
+                }
+                if (cnt) {
+                    uint32_t pos0 = 0;
+                    if (lane == 0) pos0 = atomicAdd(&s_out_n[b], cnt);
+                    pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+#pragma unroll
+                    for (int j = 0; j < J; j++) {
+                        if (bal[j]) {
+                            const bool want = m[j] >= 0;
+                            const PT pr = Pair<PB>::make(want ? R.pay((uint32_t)m[j]) : Pt(0), rows[j].pay);
+                            stage_pairs<PB, BATCH>(Q, stage, pos0 + __popc(bal[j] & lt), want, pr, join, o_first, o_cap);
+                            pos0 += __popc(bal[j]);
                         }
                     }
                 }
             } else {
-                for (uint32_t base = 0; base < ns; base += blockDim.x) {
-                    const uint32_t i = base + threadIdx.x;
-                    bool active = i < ns;
-                    Key<KW> skey;
-                    uint64_t sh = 0;
+                // Duplicate build keys: lanes walk their probe sequences in lock step and
+                // stage every match, one reservation per warp and step.
+#pragma unroll
+                for (int j = 0; j < J; j++) {
+                    bool active = r0 + c + (uint32_t)j * NC < ns;
+                    uint64_t h = 0;
                     uint32_t slot = 0;
                     if (active) {
-                        skey = Sv.key(i);
-                        sh = HS ? Sv.hash(i) : row_hash<KW>(skey, Q.hs);
-                        slot = (uint32_t)(mix_hash(sh) >> Q.slot_shift) & cmask;
+                        h = HS ? rows[j].hash : row_hash<KW>(rows[j].key, Q.hs);
+                        slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
                     }
-                    // Lanes walk their probe sequences in lock step; each step emits the lanes
-                    // that matched with one shared-memory reservation per warp. Without
-                    // duplicate build keys a probe row stops at its first match.
+                    uint32_t steps = 0;
                     while (__any_sync(0xffffffffu, active)) {
                         bool match = false;
                         Pt rp = 0;
                         if (active) {
-                            const uint32_t e = t_idx[slot];
-                            if (e == 0) {
+                            const uint32_t e = T[slot];
+                            if ((e >> 16) != tag || ++steps > cap) {
                                 active = false;
                             } else {
-                                if (key_equal<KW>(R.key(e - 1), skey) && (!HS || R.hash(e - 1) == sh)) {
+                                const uint32_t bi = (e & 0xffffu) - 1;
+                                if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == h)) {
                                     match = true;
-                                    rp = R.pay(e - 1);
-                                    active = dups;
+                                    rp = R.pay(bi);
                                 }
                                 slot = (slot + 1) & cmask;
                             }
                         }
-                        const uint32_t m = __ballot_sync(0xffffffffu, match);
-                        if (m) {
-                            const int leader = __ffs(m) - 1;
+                        const uint32_t mb = __ballot_sync(0xffffffffu, match);
+                        if (mb) {
                             uint32_t pos0 = 0;
-                            if (lane == leader) pos0 = atomicAdd(&s_out_n, (uint32_t)__popc(m));
-                            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
-                            if (match) {
-                                const uint32_t pos = pos0 + __popc(m & lanemask_lt());
-                                const Pt sp = Sv.pay(i);
-                                if (pos < Q.outcap) {
-                                    stage[pos] = Pair<PB>::make(rp, sp);
-                                } else {
-                                    // staging full (build rows with many duplicates): direct write
-                                    const unsigned long long g = atomicAdd(out_counter<BATCH>(Q, join), 1ull);
-                                    if (g < o_cap) ((PT *)Q.out)[o_first + g] = Pair<PB>::make(rp, sp);
-                                }
-                            }
+                            if (lane == 0) pos0 = atomicAdd(&s_out_n[b], (uint32_t)__popc(mb));
+                            pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+                            stage_pairs<PB, BATCH>(Q, stage, pos0 + __popc(mb & lt), match, Pair<PB>::make(rp, rows[j].pay), join, o_first, o_cap);
                         }
                     }
                 }
             }
-            rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, join, &s_pend_join, &s_flush_join);
         }
+        // staged pairs -> visible to the producer's bulk store; then hand the item back
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);
     }
-    // drain: the buffer filled last and the one before it
-    rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
-    rotate_stage<PB, BATCH>(Q, stage0, cur, &s_out_n, &s_flush_n, &s_flush_base, &s_pend_n, &s_pend_base, s_pend_join, &s_pend_join, &s_flush_join);
 }
 
 }  // namespace vj

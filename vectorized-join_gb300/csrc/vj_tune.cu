@@ -74,15 +74,6 @@ std::vector<vj_join_options> candidates(const vj_table *r, const vj_join_options
             }
         }
     }
-    if (r->rows >= (1ull << 20)) {
-        for (int bits : {9, 10}) {
-            vj_join_options o = b;
-            o.flags = VJ_JOIN_FIXED_PASSES | VJ_JOIN_L2_TABLES;
-            o.passes = 1;
-            o.radix_bits[0] = bits;
-            c.push_back(o);
-        }
-    }
     if ((int)c.size() > max_n) c.resize((size_t)max_n);
     return c;
 }

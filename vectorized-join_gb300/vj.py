@@ -96,7 +96,8 @@ class VjJoinOptions(ctypes.Structure):
         ("probe_rows", ctypes.c_int32),
         ("probe_threads", ctypes.c_int32),
         ("probe_sub_rows", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("table_load_pct", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 
@@ -106,8 +107,9 @@ def options_dict(o: "VjJoinOptions") -> dict:
         "passes": o.passes if o.flags & VJ_JOIN_FIXED_PASSES else "auto",
         "radix_bits": [o.radix_bits[0], o.radix_bits[1]],
         "build_rows": o.build_rows,
+        "probe_rows": o.probe_rows,
         "probe_threads": o.probe_threads,
-        "probe_sub_rows": o.probe_sub_rows,
+        "table_load_pct": o.table_load_pct,
     }
 
 
@@ -325,8 +327,9 @@ def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTa
     return t
 
 
-def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, probe_sub_rows: int = 0, tables: str = "auto") -> VjJoinOptions:
-    """Join options; tables: "auto", "shared" (shared-memory tables) or "l2" (L2-resident tables)."""
+def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, table_load_pct: int = 0, tables: str = "auto") -> VjJoinOptions:
+    """Join options; tables: "auto" or "shared" (shared-memory tables; "l2" is refused by the
+    library with VJ_ERR_UNSUPPORTED)."""
     o = VjJoinOptions()
     o.hash_algo = hash_algo
     o.hash_bits = hash_bits
@@ -339,7 +342,7 @@ def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, r
     o.build_rows = build_rows
     o.probe_rows = probe_rows
     o.probe_threads = probe_threads
-    o.probe_sub_rows = probe_sub_rows
+    o.table_load_pct = table_load_pct
     return o
 
 
