@@ -72,6 +72,10 @@ enum vj_hash_algo {
 };
 
 VJ_API int vj_version(void);
+/* Device and page-locked host allocations the library has made in this process (workspaces,
+ * library-owned results, staging buffers, result words). A diagnostic: a call that claims
+ * to allocate nothing, such as vj_partition_noalloc, leaves it unchanged. */
+VJ_API uint64_t vj_allocation_count(void);
 VJ_API const char *vj_status_string(int status);
 /* Copies the calling thread's last error message into buf (NUL-terminated); returns its length. */
 VJ_API size_t vj_last_error(char *buf, size_t len);
@@ -160,7 +164,9 @@ typedef struct vj_table {
  * unspecified, as in the reference. radix_bits: 1..12.
  * Histogram and exclusive offsets (2^radix_bits u64 each) go to the device arrays and/or
  * the host arrays that are not NULL; host arrays make the call synchronous, as the
- * reference's copies back to the host do (join_provider.cu:645-646).
+ * reference's copies back to the host do (join_provider.cu:645-646), and turn a kernel's
+ * error flag into VJ_ERR_DEVICE. Without host arrays the call is asynchronous: a kernel
+ * error then shows as UINT64_MAX in every histogram entry (the output is incomplete).
  */
 VJ_API int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashes_in, int hash_bits, int hash_algo, void *d_keys_out, void *d_payloads_out, void *d_hashes_out, int radix_shift, int radix_bits,
                  uint64_t *d_histogram, uint64_t *d_offsets, uint64_t *h_histogram, uint64_t *h_offsets, vj_stream_t stream);
@@ -181,7 +187,11 @@ VJ_API int vj_partition(vj_ctx *ctx, const vj_table *in, const void *d_hashes_in
  *     before anything is launched.
  *   - It runs on the calling thread's current device. The first call on each device looks
  *     up the device address of the static array (cudaGetSymbolAddress) and keeps it; make
- *     that first call before any stream capture.
+ *     that first call before any stream capture. CUDA loads modules lazily: the static array
+ *     and the module's code take their device memory at that first call, so make it before
+ *     the caller's pool reserves the device's memory (a call with rows = 0 is enough).
+ *   - Errors of its kernels are reported as vj_partition reports them: VJ_ERR_DEVICE with
+ *     host arrays, UINT64_MAX in every histogram entry without.
  *   - Every call on a device shares the one array, which keeps what the last call left in
  *     it; each call clears what must start at zero itself. Calls that overlap on the GPU
  *     (streams with no order between them, or threads without a lock) race on the array and
@@ -212,7 +222,10 @@ VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes
  * VJ_JOIN_SHARED_TABLES names that explicitly. VJ_JOIN_L2_TABLES (L2-resident tables per
  * partition after one pass) is no longer offered: it was slower than shared-memory tables
  * on every measured shape, and a join that asks for it returns VJ_ERR_UNSUPPORTED. */
-enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4 };
+/* VJ_JOIN_TEST_DEVICE_FLAG is for tests of error reporting: after the probe a kernel sets a
+ * flag in the join's device error word, as a kernel whose bounded wait ran out does, and the
+ * call returns VJ_ERR_DEVICE. */
+enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4, VJ_JOIN_TEST_DEVICE_FLAG = 1 << 16 };
 typedef struct vj_join_options {
     int32_t hash_algo;      /* VJ_HASH_*: the hash the partitions are cut from */
     int32_t hash_bits;      /* 32 or 64; 0 = 64 */
@@ -318,7 +331,8 @@ VJ_API int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, uint
  *     waited for. A join whose estimated footprint exceeds the whole budget is refused
  *     with VJ_ERR_BUDGET. Admission is in arrival order, except that a request that fits
  *     may pass a head that does not (at most 8 times per head).
- *   vj_server_wait: block until the request is done; its status is vj_join's (VJ_OK, or
+ *   vj_server_wait: block until the request is done (one waiter per request: a second
+ *     thread waiting for the same id gets VJ_ERR_INVALID_ARGUMENT); its status is vj_join's (VJ_OK, or
  *     VJ_ERR_CAPACITY with count = pairs needed), times are seconds since the server
  *     started. Each request's result equals vj_join's on the same tables.
  *   vj_server_destroy: finishes every queued request, then frees the slots.

@@ -49,10 +49,11 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> bool:
-    """Build oracle/_ref from the reference sources when they are present (this container
-    only). Returns True when the reference checkers exist afterwards."""
-    if Path(reference_root, "src", "hash", "hash.cu").exists():
+def build_ref(reference_root: str | None) -> bool:
+    """Build oracle/_ref from the reference sources under reference_root (the checkout of
+    vgerber/vectorized-join) when they are there. Returns True when the reference checkers
+    exist afterwards."""
+    if reference_root and Path(reference_root, "src", "hash", "hash.cu").exists():
         subprocess.check_call(["bash", str(HERE / "ref_build.sh"), reference_root])
     return (REF_DIR / "ref_join_cpu").exists()
 

@@ -4,9 +4,9 @@
 #   ref_hash_host_h{HB}_c{CB}  reference hash kernels run as host code (x86/Arm CPU)
 #   ref_join_cpu               reference JoinProvider::join_cpu on host tables
 #   ref_h{HB}_c{CB}.cubin      reference hash kernels for sm_103a (loaded on a GPU machine)
-# usage: oracle/ref_build.sh [reference root]   (default /root/reference)
+# usage: oracle/ref_build.sh REFERENCE_ROOT   (the checkout of vgerber/vectorized-join)
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:?usage: oracle/ref_build.sh REFERENCE_ROOT}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/hash/hash.cu" ]; then

@@ -91,3 +91,5 @@ def test_join_options_round_trip(vjlib):
     t = vjlib.options_dict(vjlib.options(probe_threads=256, table_load_pct=25, probe_rows=4096))
     assert t["probe_threads"] == 256 and t["table_load_pct"] == 25 and t["probe_rows"] == 4096
     assert ctypes.sizeof(vjlib.VjJoinOptions) == 56  # include/vj.h layout (unchanged by table_load_pct)
+    assert vjlib.options(test_device_flag=True).flags == vjlib.VJ_JOIN_TEST_DEVICE_FLAG
+    assert vjlib.allocation_count() >= 0

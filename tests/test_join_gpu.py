@@ -173,6 +173,24 @@ def test_probe_shapes_vs_oracle(vjlib, ctx, cuda, oracle):
         assert np.array_equal(sort_pairs(got), want), vjlib.options_dict(opts)
 
 
+def test_device_flag_reaches_the_status(vjlib, ctx, cuda, oracle):
+    """A flag a kernel sets in the join's error word (here planted by the test option, as a
+    bounded wait that ran out would set it) comes back as VJ_ERR_DEVICE, and the next join
+    on the same context is clean again."""
+    rng = np.random.default_rng(4)
+    rk = rng.integers(0, 2**40, size=5000, dtype=np.uint64)
+    sk = rk[rng.integers(0, 5000, size=20000)]
+    rp = np.arange(5000, dtype=np.uint64)
+    sp = np.arange(20000, dtype=np.uint64)
+    with pytest.raises(vjlib.VjError) as e:
+        gpu_join(vjlib, ctx, cuda, rk, rp, sk, sp, vjlib.options(test_device_flag=True), capacity=20000)
+    assert e.value.status == vjlib.VJ_ERR_DEVICE
+    assert "flags 20" in str(e.value)
+    cnt, want, _ = oracle.join(rk, rp, sk, sp)
+    count, got = gpu_join(vjlib, ctx, cuda, rk, rp, sk, sp, capacity=20000)
+    assert count == cnt and np.array_equal(sort_pairs(got), want)
+
+
 def test_l2_tables_flag_refused(vjlib, ctx, cuda):
     one = np.array([5], np.uint64)
     with pytest.raises(vjlib.VjError) as e:

@@ -5,11 +5,15 @@ pool, or one that cannot let a cudaFree synchronise a device its other streams a
 vj_partition_noalloc serves them: it takes no context, and the pass's working memory is a
 static device array of VJ_NOALLOC_SCRATCH_BYTES instead of a context workspace.
 
-The GPU test calls it through the C ABI twice in a row, with different layouts and bucket
-counts, so that the second call starts on the scratch contents the first call left behind.
-Each result must equal what vj_partition (the context entry point) gives for the same input:
-the same histogram and offsets, exactly, and each bucket holding the same rows (the order
-inside a bucket is unspecified for both). This file is named to be collected last.
+The GPU test first makes an empty call (rows = 0), the warm-up such a caller makes before
+its pool takes the device's memory: it places the library's module and static array on the
+device. It then calls the entry point through the C ABI twice in a row, with different
+layouts and bucket counts, so that the second call starts on the scratch contents the first
+call left behind, and checks that neither call made an allocation (the library's own
+allocation counter). Each result must equal what vj_partition (the context entry point)
+gives for the same input: the same histogram and offsets, exactly, and each bucket holding
+the same rows (the order inside a bucket is unspecified for both). This file is named to be
+collected last.
 """
 from __future__ import annotations
 
@@ -79,7 +83,15 @@ def _same_partition(got, want, bits):
 
 @pytest.mark.gpu
 def test_noalloc_partition_matches_context_partition_twice(vjlib, ctx, cuda):
+    import torch
+
     rng = np.random.default_rng(20261203)
+    # warm-up: an empty table
+    empty = torch.zeros(1, dtype=torch.int64, device=cuda)
+    warm_hist = np.full(4, 7, np.uint64)
+    vjlib.partition_noalloc(vjlib.table(empty, empty, 0, 2, 8), empty, empty, 0, 2, h_hist=warm_hist)
+    assert warm_hist.tolist() == [0, 0, 0, 0]
+    allocations = vjlib.allocation_count()
     # first call: 2^20 + 3 rows of one u64 key, FNV-1a recomputed from the keys, the most
     # buckets the scratch holds (so it runs with fewer work units than vj_partition)
     n1 = (1 << 20) + 3
@@ -93,6 +105,7 @@ def test_noalloc_partition_matches_context_partition_twice(vjlib, ctx, cuda):
     pay2 = rng.permutation(n2).astype(np.uint64)
     h2 = rng.integers(0, 2**32, size=n2, dtype=np.uint64).astype(np.uint32)
     second = _run(vjlib, ctx, cuda, keys2, pay2, h2, 32, 5, 7, noalloc=True)
+    assert vjlib.allocation_count() == allocations, "vj_partition_noalloc allocated"
 
     _same_partition(first, _run(vjlib, ctx, cuda, keys1, pay1, None, 64, 3, MAX_RADIX_BITS, noalloc=False), MAX_RADIX_BITS)
     _same_partition(second, _run(vjlib, ctx, cuda, keys2, pay2, h2, 32, 5, 7, noalloc=False), 7)

@@ -482,6 +482,8 @@ void profile_mark(vj_ctx *ctx, int mark, cudaStream_t stream);
 // Grows the context workspace to at least `bytes` (stream-ordered; contents not kept).
 int workspace_reserve(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
 int owned_alloc(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out);
+// Counts one device or page-locked host allocation made by the library (vj_allocation_count).
+void note_allocation();
 void owned_release(vj_ctx *ctx, size_t bytes);
 // Shape class of a join (vj_tune's cache key) and the tuned options for an automatic join.
 TuneKey tune_key(const vj_table *r, const vj_table *s, const vj_join_options *opt);

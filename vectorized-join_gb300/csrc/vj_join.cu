@@ -311,7 +311,12 @@ struct JoinRun {
     bool batch = false;
     uint32_t *batch_cnt = nullptr;
     uint32_t batch_parts = 1;
+    bool plant_flag = false;  // VJ_JOIN_TEST_DEVICE_FLAG
 };
+
+// VJ_JOIN_TEST_DEVICE_FLAG: sets a flag bit in the error word as a kernel that ran out of a
+// bounded wait would, so that tests can follow it to the call's status.
+__global__ void plant_flag_kernel(uint32_t *error, uint32_t bit) { atomicOr(error, bit); }
 
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
 int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
@@ -502,7 +507,7 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         VJ_CUDA(cudaGetLastError());
         batch_items_kernel<false><<<Q.joins, 256, 0, stream>>>(Q, run.batch_parts, nullptr, run.batch_cnt);
         VJ_CUDA(cudaGetLastError());
-        ctx->launches += 2;
+        ctx->launches += 3;
     } else {
         const int nb = (run.probe.np + PLAN_BLOCK - 1) / PLAN_BLOCK;
         items_count_kernel<<<nb, PLAN_BLOCK, 0, stream>>>(run.probe, run.plan_blocks);
@@ -511,7 +516,7 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         VJ_CUDA(cudaGetLastError());
         items_write_kernel<<<nb, PLAN_BLOCK, 0, stream>>>(run.probe, run.plan_blocks);
         VJ_CUDA(cudaGetLastError());
-        ctx->launches += 2;
+        ctx->launches += 3;
     }
     if (run.aos) {
         if (run.batch) probe_kernel<KW, PB, HS, true, true><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
@@ -521,8 +526,13 @@ int launch_probe(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream) {
         else probe_kernel<KW, PB, HS, false, false><<<run.probe_grid, run.threads, run.probe_smem, stream>>>(run.probe);
     }
     VJ_CUDA(cudaGetLastError());
+    ctx->launches += 1;
+    if (run.plant_flag) {
+        plant_flag_kernel<<<1, 1, 0, stream>>>(run.d_error, 32u);
+        VJ_CUDA(cudaGetLastError());
+        ctx->launches += 1;
+    }
     profile_mark(ctx, PM_PROBE_END, stream);
-    ctx->launches += 2;
     return VJ_OK;
 }
 
@@ -581,6 +591,7 @@ int read_count(vj_ctx *ctx, const JoinRun &run, cudaStream_t stream, uint64_t *c
     if (!words.host) {
         unsigned long long *h = nullptr;
         VJ_CUDA(cudaHostAlloc((void **)&h, 2 * sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable));
+        note_allocation();
         unsigned long long *d = nullptr;
         const cudaError_t e = cudaHostGetDevicePointer((void **)&d, h, 0);
         if (e != cudaSuccess) {
@@ -613,6 +624,7 @@ int probe_once(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_o
     Plan pl = make_plan<KW, PB, HS>(t.rows[0], t.rows[1], ctx->info, opt);
     *run = JoinRun{};
     VJ_TRY((prepare<KW, PB, HS>(ctx, t, pl, hs, stream, run)));
+    run->plant_flag = opt && (opt->flags & VJ_JOIN_TEST_DEVICE_FLAG);
     run->probe.out = out;
     run->probe.capacity = capacity;
     VJ_TRY((launch_probe<KW, PB, HS>(ctx, *run, stream)));
@@ -676,10 +688,12 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
 
 }  // namespace
 
-// Export of a single-segment pass result as the reference's index_t histogram/offsets.
-__global__ void export_hist_kernel(const uint32_t *begin, const uint32_t *end, int bins, unsigned long long *hist, unsigned long long *off) {
+// Export of a single-segment pass result as the reference's index_t histogram/offsets; when a
+// kernel of the pass set an error flag, every histogram entry is UINT64_MAX instead.
+__global__ void export_hist_kernel(const uint32_t *begin, const uint32_t *end, int bins, unsigned long long *hist, unsigned long long *off, const uint32_t *error) {
+    const bool bad = *error != 0;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bins; b += gridDim.x * blockDim.x) {
-        if (hist) hist[b] = end[b] - begin[b];
+        if (hist) hist[b] = bad ? ~0ull : (unsigned long long)(end[b] - begin[b]);
         if (off) off[b] = begin[b];
     }
 }
@@ -734,7 +748,7 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
         VJ_CUDA(cudaMemsetAsync(pb.part_begin, 0, bins * sizeof(uint32_t), stream));
         VJ_CUDA(cudaMemsetAsync(pb.part_end, 0, bins * sizeof(uint32_t), stream));
     }
-    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(pb.part_begin, pb.part_end, bins, d_hist ? (unsigned long long *)d_hist : dh, d_off ? (unsigned long long *)d_off : doff);
+    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(pb.part_begin, pb.part_end, bins, d_hist ? (unsigned long long *)d_hist : dh, d_off ? (unsigned long long *)d_off : doff, derr);
     VJ_CUDA(cudaGetLastError());
     if (h_hist || h_off) {
         if (h_hist) VJ_CUDA(cudaMemcpyAsync(h_hist, d_hist ? (void *)d_hist : (void *)dh, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
@@ -1534,6 +1548,7 @@ extern "C" int vj_join_host(vj_ctx *ctx, const vj_table *r, const vj_table *s, c
         }
         VJ_CHECK(!ctx->budget || ctx->owned_bytes + ctx->workspace_bytes + need <= ctx->budget, VJ_ERR_BUDGET, "vj_join_host: staging exceeds the context budget");
         VJ_CUDA(cudaMallocAsync(&ctx->stage, need, st));
+        note_allocation();
         ctx->stage_bytes = need;
     }
     Carver c;
@@ -1603,6 +1618,8 @@ char *g_noalloc_base[64];
 // Device address of the scratch on `device` (the current device), looked up on the first
 // call for that device and kept for the life of the process.
 int noalloc_scratch(int device, char **out) {
+    VJ_CHECK(device >= 0 && device < (int)(sizeof(g_noalloc_base) / sizeof(g_noalloc_base[0])), VJ_ERR_UNSUPPORTED, "vj_partition_noalloc: device %d is beyond the %d devices it keeps scratch addresses for", device,
+             (int)(sizeof(g_noalloc_base) / sizeof(g_noalloc_base[0])));
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_base[device]) {
         void *p = nullptr;
@@ -1684,7 +1701,7 @@ int partition_noalloc_typed(char *scratch, int units, const vj_table *in, const 
     }
     unsigned long long *hist = d_hist ? (unsigned long long *)d_hist : L.hist;
     unsigned long long *off = d_off ? (unsigned long long *)d_off : L.off;
-    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(L.pb.part_begin, L.pb.part_end, bins, hist, off);
+    export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(L.pb.part_begin, L.pb.part_end, bins, hist, off, L.err);
     VJ_CUDA(cudaGetLastError());
     if (h_hist || h_off) {
         if (h_hist) VJ_CUDA(cudaMemcpyAsync(h_hist, hist, bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));

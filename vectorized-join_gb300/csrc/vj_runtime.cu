@@ -1,6 +1,8 @@
 // vj_runtime.cu -- errors, context and workspace, pair digest, seeded workload generator.
 #include "vj_internal.cuh"
 
+#include <atomic>
+
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -69,17 +71,25 @@ int workspace_reserve(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out
     }
     void *p = nullptr;
     VJ_CUDA(cudaMallocAsync(&p, want, stream));
+    note_allocation();
     ctx->workspace = p;
     ctx->workspace_bytes = want;
     *out = p;
     return VJ_OK;
 }
 
+namespace {
+std::atomic<uint64_t> g_allocations{0};
+}
+
+void note_allocation() { g_allocations.fetch_add(1, std::memory_order_relaxed); }
+
 int owned_alloc(vj_ctx *ctx, size_t bytes, cudaStream_t stream, void **out) {
     uint64_t after = ctx->owned_bytes + ctx->workspace_bytes + ctx->stage_bytes + bytes;
     VJ_CHECK(!ctx->budget || after <= ctx->budget, VJ_ERR_BUDGET, "result of %zu bytes exceeds the context budget (%llu bytes)", bytes, (unsigned long long)ctx->budget);
     void *p = nullptr;
     VJ_CUDA(cudaMallocAsync(&p, bytes ? bytes : 16, stream));
+    note_allocation();
     ctx->owned_bytes += bytes;
     *out = p;
     return VJ_OK;
@@ -244,11 +254,14 @@ int host_result_scratch(unsigned long long **d, unsigned long long **h) {
     static thread_local unsigned long long *pinned = nullptr;
     int device = 0;
     VJ_CUDA(cudaGetDevice(&device));
+    VJ_CHECK(device >= 0 && device < 64, VJ_ERR_UNSUPPORTED, "device %d is beyond the 64 devices the library keeps result words for", device);
     if (!dev[device]) {
         VJ_CUDA(cudaMalloc(&dev[device], 4 * sizeof(unsigned long long)));
+        note_allocation();
     }
     if (!pinned) {
         VJ_CUDA(cudaMallocHost(&pinned, 4 * sizeof(unsigned long long)));
+        note_allocation();
     }
     *d = dev[device];
     *h = pinned;
@@ -474,3 +487,5 @@ extern "C" int vj_generate_join_expect(uint64_t seed, uint64_t nr, uint64_t ns, 
     if (h_xor) *h_xor = h[2];
     return VJ_OK;
 }
+
+extern "C" uint64_t vj_allocation_count(void) { return vj::g_allocations.load(std::memory_order_relaxed); }

@@ -37,6 +37,7 @@ struct Request {
     uint64_t need = 0;
     int bypassed = 0;
     bool done = false;
+    bool claimed = false;  // a thread is waiting for it (a second waiter is refused)
     vj_request_result res{};
 };
 
@@ -226,9 +227,11 @@ extern "C" int vj_server_wait(vj_server *srv, uint64_t request_id, vj_request_re
     auto it = srv->requests.find(request_id);
     VJ_CHECK(it != srv->requests.end(), VJ_ERR_INVALID_ARGUMENT, "vj_server_wait: unknown request %llu", (unsigned long long)request_id);
     Request *q = it->second;
+    VJ_CHECK(!q->claimed, VJ_ERR_INVALID_ARGUMENT, "vj_server_wait: request %llu is already being waited for", (unsigned long long)request_id);
+    q->claimed = true;
     srv->cv_done.wait(lock, [&] { return q->done; });
     *out = q->res;
-    srv->requests.erase(it);
+    srv->requests.erase(request_id);  // the iterator may be stale after the wait
     delete q;
     return VJ_OK;
 }

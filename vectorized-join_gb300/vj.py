@@ -23,6 +23,7 @@ VJ_ERR_BUDGET = 7
 VJ_JOIN_FIXED_PASSES = 1
 VJ_JOIN_SHARED_TABLES = 2
 VJ_JOIN_L2_TABLES = 4
+VJ_JOIN_TEST_DEVICE_FLAG = 1 << 16
 
 ALGORITHMS = [
     "fnv",
@@ -43,6 +44,7 @@ ALGORITHMS = [
 # Every symbol include/vj.h declares.
 EXPORTS = [
     "vj_version",
+    "vj_allocation_count",
     "vj_status_string",
     "vj_last_error",
     "vj_hash_algo_id",
@@ -202,6 +204,8 @@ def load() -> ctypes.CDLL:
             raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() first (no CPU fallback exists)")
         L = ctypes.CDLL(str(LIB_PATH))
         L.vj_version.restype = i32
+        L.vj_allocation_count.restype = u64
+        L.vj_allocation_count.argtypes = []
         L.vj_status_string.restype = ctypes.c_char_p
         L.vj_status_string.argtypes = [i32]
         L.vj_last_error.restype = ctypes.c_size_t
@@ -285,6 +289,11 @@ def device_to_numpy(src_ptr: int, count: int, dtype) -> "np.ndarray":
     return out
 
 
+def allocation_count() -> int:
+    """vj_allocation_count: allocations the library has made in this process."""
+    return int(load().vj_allocation_count())
+
+
 def last_error() -> str:
     buf = ctypes.create_string_buffer(512)
     load().vj_last_error(buf, len(buf))
@@ -327,13 +336,15 @@ def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTa
     return t
 
 
-def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, table_load_pct: int = 0, tables: str = "auto") -> VjJoinOptions:
+def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, table_load_pct: int = 0, tables: str = "auto", test_device_flag: bool = False) -> VjJoinOptions:
     """Join options; tables: "auto" or "shared" (shared-memory tables; "l2" is refused by the
     library with VJ_ERR_UNSUPPORTED)."""
     o = VjJoinOptions()
     o.hash_algo = hash_algo
     o.hash_bits = hash_bits
     o.flags = {"auto": 0, "shared": VJ_JOIN_SHARED_TABLES, "l2": VJ_JOIN_L2_TABLES}[tables]
+    if test_device_flag:
+        o.flags |= VJ_JOIN_TEST_DEVICE_FLAG
     if passes is not None:
         o.flags |= VJ_JOIN_FIXED_PASSES
         o.passes = passes
