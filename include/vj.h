@@ -218,7 +218,7 @@ VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes
 /* Join options (JoinConfig, src/join/join_provider.cuh:108-122). A zero-initialised struct
  * means "automatic": FNV-1a, 64-bit hash, passes, radix bits and table size from the tuner. */
 /* flags: VJ_JOIN_FIXED_PASSES takes passes and radix_bits as given. Build tables are
- * shared-memory tables per build chunk of <= 8192 rows after up to two radix passes;
+ * shared-memory tables per build chunk of <= 2048 rows after up to two radix passes;
  * VJ_JOIN_SHARED_TABLES names that explicitly. VJ_JOIN_L2_TABLES (L2-resident tables per
  * partition after one pass) is no longer offered: it was slower than shared-memory tables
  * on every measured shape, and a join that asks for it returns VJ_ERR_UNSUPPORTED. */
@@ -240,7 +240,7 @@ typedef struct vj_join_options {
                                0 = automatic (1024) */
     int32_t probe_sub_rows; /* unused (kept for layout compatibility) */
     int32_t table_load_pct; /* largest load of a build table in percent (50, 25 or 12: table
-                               slots per build row 2, 4 or 8); 0 = automatic (50) */
+                               slots per build row 2, 4 or 8); 0 = automatic (12) */
     int32_t reserved[3];
 } vj_join_options;
 

@@ -59,12 +59,41 @@ size_t probe_smem_budget(const DeviceInfo &info) {
     return per_block > 1024 ? per_block - 1024 : per_block;
 }
 
-// Table slots per build row for a requested load (percent): 2, 4 or 8.
+// Table slots per build row for a requested load (percent): 2, 4 or 8 (0: 8, load <= 1/8).
 uint32_t table_mul(int load_pct) {
-    if (load_pct <= 0) return 2;
+    if (load_pct <= 0) return 8;
     uint32_t m = 2;
     while (m < 8 && (int)(100 / m) > load_pct) m <<= 1;
     return m;
+}
+
+// Units of a pass over `rows` rows in G segments: at most 64 per SM (short units keep the
+// SMs busy as blocks finish; 16 per SM was 0.26 ms slower on the 2^27 x 2^29 join, 256 per
+// SM slower still in the scatters), none shorter than MIN_UNIT_ROWS, and one more per
+// segment (every segment has a unit, whose block writes the segment's bounds).
+constexpr uint32_t MIN_UNIT_ROWS = 4096;
+int pass_units(const DeviceInfo &info, uint64_t rows, int G) {
+    const uint64_t by_rows = (rows + MIN_UNIT_ROWS - 1) / MIN_UNIT_ROWS;
+    const uint64_t cap = (uint64_t)info.sms * 64;
+    return (int)((by_rows < cap ? by_rows : cap) + (uint64_t)G + 1);
+}
+
+// The unit plan of a pass over one or two whole tables (plan_block's rule, on the host).
+void host_plan(PassParams &P, const uint32_t *rows, int nsides) {
+    uint64_t total = 0;
+    for (int sd = 0; sd < nsides; sd++) total += rows[sd];
+    const uint64_t room = P.max_units > nsides ? (uint64_t)(P.max_units - nsides) : 1ull;
+    uint64_t t = (total + room - 1) / room;
+    if (t < P.min_unit_rows) t = P.min_unit_rows;
+    if (t < 1) t = 1;
+    const uint32_t target = (uint32_t)(t < 0x7fffffffull ? t : 0x7fffffffull);
+    P.plan = nullptr;
+    P.hplan[0] = target;
+    P.hplan[1] = 0;
+    for (int sd = 0; sd < nsides; sd++) {
+        const uint32_t n = rows[sd] ? (uint32_t)((rows[sd] + (uint64_t)target - 1) / target) : 1u;
+        P.hplan[2 + sd] = P.hplan[1 + sd] + n;
+    }
 }
 
 template <int KW, int PB, int HS>
@@ -78,13 +107,13 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     }
     pl.tmul = table_mul(opt ? opt->table_load_pct : 0);
     const size_t budget = probe_smem_budget(info);
-    // largest build chunk (a power of two) whose buffers, tables and a stage of two pairs per
-    // build row fit one block
+    // largest build chunk (a power of two, at most 2048: table slots hold 11-bit rows) whose
+    // buffers, tables and a stage of one pair per build row fit one block
     pl.rcap = 64;
-    for (uint32_t rcap = 8192; rcap >= 64; rcap >>= 1) {
+    for (uint32_t rcap = 2048; rcap >= 64; rcap >>= 1) {
         uint32_t tcap = 64;
         while (tcap < rcap * pl.tmul) tcap <<= 1;
-        if (tcap <= 16384 && SMf::bytes(rcap, tcap, 2 * rcap) <= budget) {
+        if (tcap <= 16384 && SMf::bytes(rcap, tcap, rcap) <= budget) {
             pl.rcap = rcap;
             break;
         }
@@ -131,12 +160,8 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     for (int p = 0; p < 2; p++) {
         if (pl.bits[p] > MAX_RADIX_BITS) pl.bits[p] = MAX_RADIX_BITS;
     }
-    const int G0 = 2;
-    const int G1 = 2 << pl.bits[0];
-    // 64 work units per SM: short units keep the SMs full as blocks finish (16 per SM was
-    // 0.26 ms slower on the 2^27 x 2^29 join, 256 per SM slower still in the scatters)
-    pl.max_units[0] = info.sms * 64 + G0;
-    pl.max_units[1] = info.sms * 64 + G1;
+    pl.max_units[0] = pass_units(info, nr + ns, 2);
+    pl.max_units[1] = pass_units(info, nr + ns, 2 << pl.bits[0]);
     return pl;
 }
 
@@ -180,57 +205,63 @@ int blocks_per_sm(K kernel, int threads, size_t smem, int *per_sm) {
 }
 
 
+// Bookkeeping of one pass (workspace).
 struct PassBufs {
-    uint4 *units;
-    uint32_t *unit_count, *seg_first_unit, *cnt, *seg_tot, *unit_off, *part_begin, *part_end;
+    uint32_t *plan = nullptr;              // [G + 2]: the pass's unit plan when the previous pass writes it
+    uint32_t *ctl = nullptr;               // [4]: counters and the scatter's ticket \  cleared
+    uint32_t *seg_done = nullptr;          // [G]: units counted per segment          |  before
+    uint32_t *seg_tot = nullptr;           // [G * bins]: bucket totals per segment   /  the pass
+    unsigned long long *look = nullptr;    // [max_units * bins]: look-back words
+    uint32_t *part_begin = nullptr, *part_end = nullptr;  // [G * bins]
+    int max_units = 0;
+    int G = 0;
 };
 
 PassBufs carve_pass(Carver &c, int G, int bins, int max_units) {
     PassBufs b;
-    b.units = c.take<uint4>(max_units);
-    b.unit_count = c.take<uint32_t>(1);
-    b.seg_first_unit = c.take<uint32_t>(G);
-    b.cnt = c.take<uint32_t>((size_t)max_units * bins);
-    b.seg_tot = c.take<uint32_t>((size_t)G * bins);
-    b.unit_off = c.take<uint32_t>((size_t)max_units * bins);
+    b.plan = c.take<uint32_t>((size_t)G + 2);
+    b.ctl = c.take<uint32_t>(4);
+    b.seg_done = c.take<uint32_t>((size_t)G, 16);
+    b.seg_tot = c.take<uint32_t>((size_t)G * bins, 16);
+    b.look = c.take<unsigned long long>((size_t)max_units * bins);
     b.part_begin = c.take<uint32_t>((size_t)G * bins);
     b.part_end = c.take<uint32_t>((size_t)G * bins);
+    b.max_units = max_units;
+    b.G = G;
     return b;
 }
 
+// One radix pass: histogram (per-unit counts, partition bounds, the next pass's plan) and
+// scatter (look-back cursors, bucket-sorted tiles). P's plan (device or host), sides,
+// segments, bucket rule and next_plan are the caller's; the bookkeeping comes from b.
 template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS>
-int run_pass(vj_ctx *ctx, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
-    const int G = P.nsides * P.Q;
+int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
     const uint32_t bins = 1u << P.bits;
-    P.units = b.units;
-    P.unit_count = b.unit_count;
-    P.seg_first_unit = b.seg_first_unit;
-    P.cnt = b.cnt;
+    P.ctl = b.ctl;
+    P.seg_done = b.seg_done;
     P.seg_tot = b.seg_tot;
-    P.unit_off = b.unit_off;
+    P.look = b.look;
     P.part_begin = b.part_begin;
     P.part_end = b.part_end;
-    VJ_CUDA(cudaMemsetAsync(b.seg_tot, 0, (size_t)G * bins * sizeof(uint32_t), stream));
-    plan_units_kernel<<<1, PLAN_THREADS, 0, stream>>>(P);
-    VJ_CUDA(cudaGetLastError());
+    P.max_units = b.max_units;
     profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
-    histogram_kernel<KW, PB, HS, IN_AOS><<<P.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    // counters, ticket and the segments' totals start at zero (the histogram writes every
+    // unit's look-back words)
+    VJ_CUDA(cudaMemsetAsync(b.ctl, 0, (size_t)((char *)(b.seg_tot + (size_t)b.G * bins) - (char *)b.ctl), stream));
+    histogram_kernel<KW, PB, HS, IN_AOS><<<b.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_HIST_END + 4 * pass, stream);
-    seg_scan_kernel<<<G, PART_THREADS, 0, stream>>>(P);
-    VJ_CUDA(cudaGetLastError());
-    const size_t us_smem = (size_t)P.max_units * sizeof(uint32_t);
-    VJ_TRY(ensure_smem(unit_scan_kernel, us_smem));
-    unit_scan_kernel<<<bins, PLAN_THREADS, us_smem, stream>>>(P);
-    VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCAN_END + 4 * pass, stream);
     constexpr int ITEMS = scatter_items<KW, PB, HS, IN_AOS>();
     const size_t sc_smem = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS>::bytes(bins);
     VJ_TRY(ensure_smem(scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS>, sc_smem));
-    scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS><<<P.max_units, PART_THREADS, sc_smem, stream>>>(P);
+    int per_sm = 0;
+    VJ_TRY(blocks_per_sm(scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS>, PART_THREADS, sc_smem, &per_sm));
+    VJ_CHECK(per_sm >= 1, VJ_ERR_UNSUPPORTED, "scatter kernel does not fit an SM (%zu bytes of shared memory)", sc_smem);
+    scatter_kernel<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS><<<sms * per_sm, PART_THREADS, sc_smem, stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_SCATTER_END + 4 * pass, stream);
-    if (ctx) ctx->launches += 5;
+    if (ctx) ctx->launches += 2;
     return VJ_OK;
 }
 
@@ -341,8 +372,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     const int np = J * (pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1));
     int max_units[2] = {pl.max_units[0], pl.max_units[1]};
     if (batch) {
-        max_units[0] = ctx->info.sms * 64 + G0;
-        max_units[1] = ctx->info.sms * 64 + G1;
+        max_units[0] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G0);
+        max_units[1] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G1);
     }
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
@@ -427,13 +458,27 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         P.shift = 64 - consumed_bits;  // top bits of the mixed hash, pass 1 first
         P.hs = hs;
         P.max_units = max_units[pass];
-        P.min_unit_rows = 4096;
+        P.min_unit_rows = MIN_UNIT_ROWS;
         P.error = error;
         const PassBufs &pb = pass == 0 ? pb0 : pb1;
-        if (pass == 0) {
-            VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, pass, P, pb, stream)));
+        if (pass == 0 && !batch) {
+            host_plan(P, in.rows, 2);
         } else {
-            VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, pass, P, pb, stream)));
+            P.plan = pb.plan;  // written by the previous pass, or by plan_kernel for a batch
+            if (pass == 0) {
+                plan_kernel<<<1, PLAN_THREADS, 0, stream>>>(P, pb.plan);
+                VJ_CUDA(cudaGetLastError());
+                ctx->launches += 1;
+            }
+        }
+        if (pass == 0 && pl.passes >= 2) {
+            P.next_plan = pb1.plan;
+            P.next_max_units = pb1.max_units;
+        }
+        if (pass == 0) {
+            VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, ctx->info.sms, pass, P, pb, stream)));
+        } else {
+            VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, ctx->info.sms, pass, P, pb, stream)));
         }
         seg_begin = pb.part_begin;
         seg_end = pb.part_end;
@@ -705,7 +750,7 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
                     uint64_t *h_hist, uint64_t *h_off, cudaStream_t stream) {
     const int bins = 1 << bits;
     const int G = 1;
-    const int max_units = ctx->info.sms * 16 + G;
+    const int max_units = pass_units(ctx->info, in->rows, G);
     auto layout = [&](Carver &c, PassBufs *pb, unsigned long long **hist, unsigned long long **off, uint32_t **err) {
         *pb = carve_pass(c, G, bins, max_units);
         *hist = c.take<unsigned long long>(bins);
@@ -740,14 +785,12 @@ int partition_typed(vj_ctx *ctx, const vj_table *in, const void *hashes_in, cons
     P.bits = bits;
     P.hs = hs;
     P.max_units = max_units;
-    P.min_unit_rows = 4096;
+    P.min_unit_rows = MIN_UNIT_ROWS;
     P.error = derr;
-    if (in->rows > 0) {
-        VJ_TRY((run_pass<KW, PB, HS, false, false>(ctx, 0, P, pb, stream)));
-    } else {
-        VJ_CUDA(cudaMemsetAsync(pb.part_begin, 0, bins * sizeof(uint32_t), stream));
-        VJ_CUDA(cudaMemsetAsync(pb.part_end, 0, bins * sizeof(uint32_t), stream));
-    }
+    const uint32_t rows = (uint32_t)in->rows;
+    host_plan(P, &rows, 1);
+    // an empty table still has one (empty) unit, which writes the empty bounds
+    VJ_TRY((run_pass<KW, PB, HS, false, false>(ctx, ctx->info.sms, 0, P, pb, stream)));
     export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(pb.part_begin, pb.part_end, bins, d_hist ? (unsigned long long *)d_hist : dh, d_off ? (unsigned long long *)d_off : doff, derr);
     VJ_CUDA(cudaGetLastError());
     if (h_hist || h_off) {
@@ -1240,12 +1283,13 @@ struct ChunkJoinerT final : ChunkJoiner {
     unsigned long long *plan_blocks = nullptr, *out_count = nullptr;
     uint64_t item_cap = 0;
 
-    int units(int pass) const { return ctx->info.sms * 64 + (pass == 0 ? 1 : (1 << pl.bits[0])); }
-
     void carve_side(Carver &c, uint32_t rows, SideBufs *b) const {
         for (int pass = 0; pass < 2; pass++) b->rows[pass] = pl.passes > pass ? c.take<char>((size_t)rows * L::STRIDE + 64) : nullptr;
         b->bids = pl.passes >= 2 ? c.take<uint16_t>((size_t)rows + 8) : nullptr;
-        for (int pass = 0; pass < pl.passes; pass++) b->pb[pass] = carve_pass(c, pass == 0 ? 1 : 1 << pl.bits[0], 1 << pl.bits[pass], units(pass));
+        for (int pass = 0; pass < pl.passes; pass++) {
+            const int G = pass == 0 ? 1 : 1 << pl.bits[0];
+            b->pb[pass] = carve_pass(c, G, 1 << pl.bits[pass], pass_units(ctx->info, rows, G));
+        }
     }
 
     void layout(Carver &c) {
@@ -1284,13 +1328,19 @@ struct ChunkJoinerT final : ChunkJoiner {
             consumed += pl.bits[pass];
             P.shift = 64 - consumed;
             P.hs = hs;
-            P.max_units = units(pass);
-            P.min_unit_rows = 4096;
+            P.max_units = b.pb[pass].max_units;
+            P.min_unit_rows = MIN_UNIT_ROWS;
             P.error = error;
             if (pass == 0) {
-                VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, pass, P, b.pb[0], stream)));
+                host_plan(P, &rows, 1);
+                if (pl.passes >= 2) {
+                    P.next_plan = b.pb[1].plan;
+                    P.next_max_units = b.pb[1].max_units;
+                }
+                VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, ctx->info.sms, pass, P, b.pb[0], stream)));
             } else {
-                VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, pass, P, b.pb[1], stream)));
+                P.plan = b.pb[1].plan;
+                VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, ctx->info.sms, pass, P, b.pb[1], stream)));
             }
             seg_begin = b.pb[pass].part_begin;
             seg_end = b.pb[pass].part_end;
@@ -1648,31 +1698,33 @@ NoallocLayout noalloc_layout(Carver &c, int bins, int units) {
     return L;
 }
 
-// Work units of the pass: as many as vj_partition uses (16 per SM), fewer when their
-// bucket counts and offsets (8 bytes per bucket per unit) would not fit in the scratch.
+// Work units of the pass: as many as vj_partition uses for these rows, fewer when their
+// look-back words (8 bytes per bucket per unit) would not fit in the scratch.
 // 0: not even two units fit.
-int noalloc_units(int sms, int bins) {
+int noalloc_units(const DeviceInfo &info, uint64_t rows, int bins) {
     Carver fixed;
     noalloc_layout(fixed, bins, 0);
-    const size_t per_unit = sizeof(uint4) + 2 * sizeof(uint32_t) * (size_t)bins;
-    const size_t slack = 3 * 256;  // alignment of the three per-unit arrays
+    const size_t per_unit = sizeof(unsigned long long) * (size_t)bins;
+    const size_t slack = 256;  // alignment of the per-unit array
     const size_t room = VJ_NOALLOC_SCRATCH_BYTES > fixed.off + slack ? VJ_NOALLOC_SCRATCH_BYTES - fixed.off - slack : 0;
     size_t units = room / per_unit;
-    if (units > (size_t)sms * 16 + 1) units = (size_t)sms * 16 + 1;
+    const size_t want = (size_t)pass_units(info, rows, 1);
+    if (units > want) units = want;
     Carver check;
     noalloc_layout(check, bins, (int)units);
     return units >= 2 && check.off <= VJ_NOALLOC_SCRATCH_BYTES ? (int)units : 0;
 }
 
 template <int KW, int PB, int HS>
-int partition_noalloc_typed(char *scratch, int units, const vj_table *in, const void *hashes_in, const HashSpec &hs, void *keys_out, void *pay_out, void *hash_out, int shift, int bits, uint64_t *d_hist,
+int partition_noalloc_typed(char *scratch, int sms, int units, const vj_table *in, const void *hashes_in, const HashSpec &hs, void *keys_out, void *pay_out, void *hash_out, int shift, int bits, uint64_t *d_hist,
                             uint64_t *d_off, uint64_t *h_hist, uint64_t *h_off, cudaStream_t stream) {
     const int bins = 1 << bits;
     Carver c;
     c.base = scratch;
     const NoallocLayout L = noalloc_layout(c, bins, units);
     // The scratch holds whatever the previous call left. The error flag must start at zero;
-    // the pass clears its own bucket totals and overwrites every other array before use.
+    // the pass clears its own counters and bucket totals and overwrites every other array
+    // before use.
     VJ_CUDA(cudaMemsetAsync(L.err, 0, sizeof(uint32_t), stream));
     PassParams P{};
     P.side[0].keys_in = in->keys;
@@ -1691,14 +1743,12 @@ int partition_noalloc_typed(char *scratch, int units, const vj_table *in, const 
     P.bits = bits;
     P.hs = hs;
     P.max_units = units;
-    P.min_unit_rows = 4096;
+    P.min_unit_rows = MIN_UNIT_ROWS;
     P.error = L.err;
-    if (in->rows > 0) {
-        VJ_TRY((run_pass<KW, PB, HS, false, false>(nullptr, 0, P, L.pb, stream)));
-    } else {
-        VJ_CUDA(cudaMemsetAsync(L.pb.part_begin, 0, bins * sizeof(uint32_t), stream));
-        VJ_CUDA(cudaMemsetAsync(L.pb.part_end, 0, bins * sizeof(uint32_t), stream));
-    }
+    const uint32_t rows = (uint32_t)in->rows;
+    host_plan(P, &rows, 1);
+    // an empty table still has one (empty) unit, which writes the empty bounds
+    VJ_TRY((run_pass<KW, PB, HS, false, false>(nullptr, sms, 0, P, L.pb, stream)));
     unsigned long long *hist = d_hist ? (unsigned long long *)d_hist : L.hist;
     unsigned long long *off = d_off ? (unsigned long long *)d_off : L.off;
     export_hist_kernel<<<(bins + 255) / 256, 256, 0, stream>>>(L.pb.part_begin, L.pb.part_end, bins, hist, off, L.err);
@@ -1716,6 +1766,7 @@ int partition_noalloc_typed(char *scratch, int units, const vj_table *in, const 
 
 struct NoallocPartitionCall {
     char *scratch;
+    int sms;
     int units;
     const vj_table *in;
     const void *hashes;
@@ -1726,7 +1777,7 @@ struct NoallocPartitionCall {
     cudaStream_t stream;
     template <int KW, int PB, int HS>
     int run() {
-        return partition_noalloc_typed<KW, PB, HS>(scratch, units, in, hashes, hs, ko, po, ho, shift, bits, dh, doff, hh, hoff, stream);
+        return partition_noalloc_typed<KW, PB, HS>(scratch, sms, units, in, hashes, hs, ko, po, ho, shift, bits, dh, doff, hh, hoff, stream);
     }
 };
 
@@ -1750,7 +1801,8 @@ extern "C" int vj_partition_noalloc(const vj_table *in, const void *d_hashes_in,
     VJ_TRY(device_info(device, &info));
     NoallocPartitionCall call;
     VJ_TRY(noalloc_scratch(device, &call.scratch));
-    call.units = noalloc_units(info.sms, 1 << radix_bits);
+    call.sms = info.sms;
+    call.units = noalloc_units(info, in->rows, 1 << radix_bits);
     VJ_CHECK(call.units > 0, VJ_ERR_UNSUPPORTED, "vj_partition_noalloc: %d buckets do not fit the %u-byte static scratch", 1 << radix_bits, (unsigned)VJ_NOALLOC_SCRATCH_BYTES);
     call.in = in;
     call.hashes = d_hashes_in;

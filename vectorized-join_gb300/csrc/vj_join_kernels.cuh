@@ -9,14 +9,10 @@
 // (a few integer ops per row).
 //
 // A pass over a set of "segments" (contiguous row ranges, e.g. the partitions of the
-// previous pass) runs five kernels, none of which waits on another block:
-//   plan_units   split segments into units of similar size (one block)
-//   histogram    per-unit bucket counts in shared memory
-//   seg_scan     per-segment exclusive prefix over buckets -> partition boundaries
-//   unit_scan    per-bucket prefix over units -> each unit's write cursor per bucket
-//   scatter      bulk copies stream tiles of a unit into shared memory (double
-//                buffered); each tile is ranked by bucket, sorted in shared memory and
-//                written out as one contiguous run per bucket
+// previous pass) runs two kernels (see "partition kernels" below): a histogram that counts
+// units of rows per bucket and writes the partition bounds, and a persistent scatter that
+// finds each unit's write cursors by decoupled look-back over the units' counts, sorts
+// tiles by bucket in shared memory and writes bucket runs as contiguous bursts.
 // The probe stage plans (partition, build chunk, probe chunk) work items and runs a
 // persistent kernel in which one warp fetches items, copies their build rows in and
 // flushes their pairs out, while the other warps build shared-memory tables and probe
@@ -71,24 +67,31 @@ struct Side {
 struct PassParams {
     Side side[2];
     int nsides;
-    int Q;                       // segments per side
-    const uint32_t *seg_begin;   // [nsides*Q], null: one segment = the whole side
+    int Q;                       // segments per side (G = nsides * Q)
+    const uint32_t *seg_begin;   // [G], null: one segment = the whole side
     const uint32_t *seg_end;
     int shift;                   // bucket = (hash >> shift) & (2^bits - 1)
     int bits;
     HashSpec hs;
-    uint4 *units;                // (segment, begin, end, side)
-    uint32_t *unit_count;
-    uint32_t *seg_first_unit;    // [G]
+    int next_shift, next_bits;   // bucket of the next pass (bid_out)
+    // Units: segment g's rows are cut into units of `target` rows (its last one shorter, at
+    // least one unit per segment); units [first[g], first[g + 1]) belong to segment g. The
+    // plan (target, first[0..G]) is `plan` on the device or, when plan is null, hplan
+    // (G <= 2, planned on the host).
+    const uint32_t *plan;
+    uint32_t hplan[4];
     int max_units;
     uint32_t min_unit_rows;
-    uint32_t *cnt;               // [max_units][bins]
-    uint32_t *seg_tot;           // [G][bins]
-    uint32_t *unit_off;          // [max_units][bins]
+    uint32_t *ctl;               // [4], zero before the pass: units counted, scatter ticket
+    uint32_t *seg_done;          // [G], zero before the pass: units counted per segment
+    uint32_t *seg_tot;           // [G*bins], zero before the pass: the segments' bucket totals
+    unsigned long long *look;    // [max_units][bins]: look-back words (flag | value)
     uint32_t *part_begin;        // [G*bins]
     uint32_t *part_end;          // [G*bins]
     uint32_t *error;             // bit 4: a bulk-copy wait ran out
-    int next_shift, next_bits;   // bucket of the next pass (bid_out)
+    // the next pass's plan over this pass's partitions (written by the unit counted last)
+    uint32_t *next_plan;         // [G*bins + 2] or null
+    int next_max_units;
 };
 
 struct ProbeParams {
@@ -160,15 +163,6 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T *total) {
     if (total) *total = warp_sums[nwarps - 1];
     __syncthreads();
     return result;
-}
-
-// One thread polls the mbarrier, the block waits on a barrier behind it (the barrier
-// orders the other threads' reads after the poller's acquire). Returns false for every
-// thread if the bounded poll ran out.
-__device__ __forceinline__ bool block_wait(uint64_t *bar, uint32_t parity) {
-    int fail = 0;
-    if (threadIdx.x == 0) fail = !mbar_wait(bar, parity);
-    return __syncthreads_or(fail) == 0;
 }
 
 // Generic (non-FNV) row hash, out of line.
@@ -341,49 +335,120 @@ struct Chunk {
 };
 
 // ------------------------------------------------------------------ partition kernels
+//
+// A pass over G segments runs two kernels:
+//   histogram  each block counts one unit (a row range of one segment) per bucket in shared
+//              memory and publishes the counts as the unit's look-back words; the segment's
+//              bucket totals add up in global memory. The block that counts a segment's last
+//              unit turns its totals into partition bounds, and the block that counts the
+//              last unit of all plans the next pass's units over those partitions.
+//   scatter    persistent; blocks take units by ticket, in order. A unit's write cursor per
+//              bucket is its partition's begin plus the rows of the segment's earlier units
+//              in that bucket, found by decoupled look-back: a predecessor's word holds
+//              either its own count or, once that unit has looked back itself, its inclusive
+//              prefix, so a walk stops at the nearest inclusive prefix. The block then
+//              streams the unit's rows through shared memory in tiles (bulk copies, double
+//              buffered across units), ranks each tile by bucket, sorts it in shared memory
+//              and writes each bucket run as one contiguous burst.
 
-// One block. Splits the G segments into units of at most `target` rows.
-__global__ void __launch_bounds__(PLAN_THREADS) plan_units_kernel(PassParams P) {
-    __shared__ unsigned long long s_warp64[32];
-    __shared__ uint32_t s_warp32[32];
-    const int G = P.nsides * P.Q;
-    const int per = (G + PLAN_THREADS - 1) / PLAN_THREADS;
-    const int g0 = threadIdx.x * per;
-    unsigned long long my_rows = 0;
-    for (int g = g0; g < g0 + per && g < G; g++) {
-        const int side = g / P.Q;
-        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
-        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
-        my_rows += e - b;
+// Look-back words: flag (2 bits) | value (62 bits).
+constexpr unsigned long long LB_AGG = 1, LB_INC = 2;
+constexpr unsigned long long LB_VALUE = (1ull << 62) - 1;
+__device__ __forceinline__ unsigned long long lb_pack(unsigned long long flag, unsigned long long v) { return (flag << 62) | v; }
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v) { asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory"); }
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Unit u of a pass: segment g (of side `side`), rows [a, b); its index in the segment and
+// whether it is the segment's first / last unit.
+struct UnitRange {
+    uint32_t g, side, a, b, rank;
+    bool first, last;
+};
+
+__device__ __forceinline__ const uint32_t *plan_first(const PassParams &P) { return P.plan ? P.plan + 1 : P.hplan + 1; }
+
+__device__ __forceinline__ uint32_t plan_total(const PassParams &P) { return plan_first(P)[P.nsides * P.Q]; }
+
+// Units of segment g.
+__device__ __forceinline__ uint32_t seg_units(const PassParams &P, uint32_t g) {
+    const uint32_t *first = plan_first(P);
+    return first[g + 1] - first[g];
+}
+
+__device__ __forceinline__ UnitRange unit_range(const PassParams &P, uint32_t u) {
+    const uint32_t G = (uint32_t)(P.nsides * P.Q);
+    const uint32_t *first = plan_first(P);
+    const uint32_t target = P.plan ? P.plan[0] : P.hplan[0];
+    uint32_t lo = 0, hi = G - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= u) lo = mid;
+        else hi = mid - 1;
     }
+    const uint32_t g = lo, f0 = first[g], f1 = first[g + 1];
+    UnitRange r;
+    r.g = g;
+    r.side = g / (uint32_t)P.Q;
+    const uint32_t sb = P.seg_begin ? P.seg_begin[g] : 0;
+    const uint32_t se = P.seg_end ? P.seg_end[g] : P.side[r.side].rows;
+    const unsigned long long a = (unsigned long long)sb + (unsigned long long)(u - f0) * target;
+    r.a = (uint32_t)(a < se ? a : se);
+    r.b = (uint32_t)(a + target < se ? a + target : se);
+    r.rank = u - f0;
+    r.first = u == f0;
+    r.last = u + 1 == f1;
+    return r;
+}
+
+// One block: units of `target` rows for the G segments [begin[g], end[g]) -- at least one per
+// segment, so that every segment's bounds are written by its last unit. plan[0] = target,
+// plan[1 + g] = the first unit of g, plan[1 + G] = all units. target is the larger of
+// min_rows and the rows that spread the segments over max_units - G units.
+__device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t G, uint32_t max_units, uint32_t min_rows, uint32_t *plan) {
+    __shared__ unsigned long long s_w64[32];
+    __shared__ uint32_t s_w32[32];
+    __shared__ uint32_t s_target;
+    const uint32_t per = (G + blockDim.x - 1) / blockDim.x;
+    const uint32_t g0 = threadIdx.x * per;
+    unsigned long long rows = 0;
+    for (uint32_t g = g0; g < g0 + per && g < G; g++) rows += end[g] - begin[g];
     unsigned long long total = 0;
-    block_exclusive_scan<unsigned long long>(my_rows, s_warp64, &total);
-    const unsigned long long budget = P.max_units > G ? (unsigned long long)(P.max_units - G) : 1ull;
-    unsigned long long target = (total + budget - 1) / budget;
-    if (target < P.min_unit_rows) target = P.min_unit_rows;
-    if (target < 1) target = 1;
-    uint32_t my_units = 0;
-    for (int g = g0; g < g0 + per && g < G; g++) {
-        const int side = g / P.Q;
-        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
-        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
-        my_units += (uint32_t)(((unsigned long long)(e - b) + target - 1) / target);
+    block_exclusive_scan<unsigned long long>(rows, s_w64, &total);
+    if (threadIdx.x == 0) {
+        const unsigned long long room = max_units > G ? (unsigned long long)(max_units - G) : 1ull;
+        unsigned long long t = (total + room - 1) / room;
+        if (t < min_rows) t = min_rows;
+        if (t < 1) t = 1;
+        if (t > 0x7fffffffull) t = 0x7fffffffull;
+        s_target = (uint32_t)t;
     }
-    uint32_t units_total = 0;
-    uint32_t first = block_exclusive_scan<uint32_t>(my_units, s_warp32, &units_total);
-    for (int g = g0; g < g0 + per && g < G; g++) {
-        const int side = g / P.Q;
-        uint32_t b = P.seg_begin ? P.seg_begin[g] : 0;
-        uint32_t e = P.seg_end ? P.seg_end[g] : P.side[side].rows;
-        P.seg_first_unit[g] = first;
-        for (unsigned long long x = b; x < e; x += target) {
-            unsigned long long xe = x + target < e ? x + target : e;
-            P.units[first++] = make_uint4((uint32_t)g, (uint32_t)x, (uint32_t)xe, (uint32_t)side);
-        }
+    __syncthreads();
+    const uint32_t target = s_target;
+    uint32_t mine = 0;
+    for (uint32_t g = g0; g < g0 + per && g < G; g++) {
+        const uint32_t n = end[g] - begin[g];
+        mine += n ? (n + target - 1) / target : 1u;
+    }
+    uint32_t units = 0;
+    uint32_t run = block_exclusive_scan<uint32_t>(mine, s_w32, &units);
+    for (uint32_t g = g0; g < g0 + per && g < G; g++) {
+        plan[1 + g] = run;
+        const uint32_t n = end[g] - begin[g];
+        run += n ? (n + target - 1) / target : 1u;
     }
     if (threadIdx.x == 0) {
-        *P.unit_count = units_total;
+        plan[0] = target;
+        plan[1 + G] = units;
     }
+}
+
+// One block: the unit plan of a pass over device segments (batches of joins).
+__global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(PassParams P, uint32_t *plan) {
+    plan_block(P.seg_begin, P.seg_end, (uint32_t)(P.nsides * P.Q), (uint32_t)P.max_units, P.min_unit_rows, plan);
 }
 
 // L2 prefetch of what the histogram reads of rows [a, b): the hash or key column, or the rows.
@@ -421,126 +486,208 @@ __device__ __forceinline__ uint64_t global_row_hash(const Side &S, uint32_t i, c
     return row_hash<KW>(load_key_stream<KW>(S.keys_in, i), hs);
 }
 
+// Grid: one block per unit of the plan (blocks past the plan's units leave at once).
 template <int KW, int PB, int HS, bool AOS>
 __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
     extern __shared__ uint32_t s_hist[];
-    const uint32_t u = blockIdx.x;
-    if (u >= *P.unit_count) return;
-    const uint4 U = P.units[u];
-    const Side &S = P.side[U.w];
+    __shared__ uint32_t s_last;
+    __shared__ uint32_t s_warp[32];
     const uint32_t bins = 1u << P.bits;
     const uint64_t mask = bins - 1;
+    const uint32_t u = blockIdx.x;
+    const uint32_t total = plan_total(P);
+    if (u >= total) return;
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
     __syncthreads();
+    const UnitRange U = unit_range(P, u);
+    const Side &S = P.side[U.side];
+
+    // ---- count
     if (S.bid_in) {
         // buckets written by the previous pass: 2 bytes a row instead of the row
         constexpr int UB = 8;
-        uint32_t i = U.y + threadIdx.x;
-        for (; i + (UB - 1) * PART_THREADS < U.z; i += UB * PART_THREADS) {
+        uint32_t i = U.a + threadIdx.x;
+        for (; i + (UB - 1) * PART_THREADS < U.b; i += UB * PART_THREADS) {
             uint32_t v[UB];
 #pragma unroll
             for (int k = 0; k < UB; k++) v[k] = __ldcs(S.bid_in + i + k * PART_THREADS);
 #pragma unroll
             for (int k = 0; k < UB; k++) atomicAdd(&s_hist[v[k] & mask], 1u);
         }
-        for (; i < U.z; i += PART_THREADS) atomicAdd(&s_hist[__ldcs(S.bid_in + i) & mask], 1u);
-        __syncthreads();
-        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
-            uint32_t c = s_hist[b];
-            P.cnt[(size_t)u * bins + b] = c;
-            if (c) atomicAdd(&P.seg_tot[(size_t)U.x * bins + b], c);
-        }
-        return;
-    }
-    constexpr int UNROLL = 4;
-    constexpr uint32_t STEP = UNROLL * PART_THREADS;
-    // keep the next AHEAD steps of this unit on their way to L2
-    constexpr uint32_t AHEAD = 4;
-    if (threadIdx.x == 0) histogram_prefetch<KW, PB, HS, AOS>(S, U.y, min(U.z, U.y + AHEAD * STEP));
-    uint32_t i = U.y + threadIdx.x;
-    for (; i + (UNROLL - 1) * PART_THREADS < U.z; i += UNROLL * PART_THREADS) {
-        if (threadIdx.x == 0) {
-            const uint32_t pa = i + AHEAD * STEP;
-            if (pa < U.z) histogram_prefetch<KW, PB, HS, AOS>(S, pa, min(U.z, pa + STEP));
-        }
-        uint64_t h[UNROLL];
+        for (; i < U.b; i += PART_THREADS) atomicAdd(&s_hist[__ldcs(S.bid_in + i) & mask], 1u);
+    } else {
+        constexpr int UNROLL = 4;
+        constexpr uint32_t STEP = UNROLL * PART_THREADS;
+        // keep the next AHEAD steps of this unit on their way to L2
+        constexpr uint32_t AHEAD = 4;
+        if (threadIdx.x == 0) histogram_prefetch<KW, PB, HS, AOS>(S, U.a, min(U.b, U.a + AHEAD * STEP));
+        uint32_t i = U.a + threadIdx.x;
+        for (; i + (UNROLL - 1) * PART_THREADS < U.b; i += UNROLL * PART_THREADS) {
+            if (threadIdx.x == 0) {
+                const uint32_t pa = i + AHEAD * STEP;
+                if (pa < U.b) histogram_prefetch<KW, PB, HS, AOS>(S, pa, min(U.b, pa + STEP));
+            }
+            uint64_t h[UNROLL];
 #pragma unroll
-        for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * PART_THREADS, P.hs);
+            for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * PART_THREADS, P.hs);
 #pragma unroll
-        for (int k = 0; k < UNROLL; k++) atomicAdd(&s_hist[(bucket_hash(h[k], P.hs) >> P.shift) & mask], 1u);
-    }
-    for (; i < U.z; i += PART_THREADS) {
-        atomicAdd(&s_hist[(bucket_hash(global_row_hash<KW, PB, HS, AOS>(S, i, P.hs), P.hs) >> P.shift) & mask], 1u);
+            for (int k = 0; k < UNROLL; k++) atomicAdd(&s_hist[(bucket_hash(h[k], P.hs) >> P.shift) & mask], 1u);
+        }
+        for (; i < U.b; i += PART_THREADS) {
+            atomicAdd(&s_hist[(bucket_hash(global_row_hash<KW, PB, HS, AOS>(S, i, P.hs), P.hs) >> P.shift) & mask], 1u);
+        }
     }
     __syncthreads();
+
+    // ---- publish: the unit's counts (its look-back words; the segment's first unit's are
+    // already its inclusive prefix) and the segment's totals
+    unsigned long long *L = P.look + (size_t)u * bins;
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
-        uint32_t c = s_hist[b];
-        P.cnt[(size_t)u * bins + b] = c;
-        if (c) atomicAdd(&P.seg_tot[(size_t)U.x * bins + b], c);
+        const uint32_t c = s_hist[b];
+        L[b] = lb_pack(U.first ? LB_INC : LB_AGG, c);
+        if (c) atomicAdd(&P.seg_tot[(size_t)U.g * bins + b], c);
     }
-}
-
-// Grid: one block per segment. Partition boundaries of every (segment, bucket).
-__global__ void __launch_bounds__(PART_THREADS) seg_scan_kernel(PassParams P) {
-    __shared__ uint32_t s_warp[32];
-    const int g = blockIdx.x;
-    const uint32_t bins = 1u << P.bits;
-    const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
-    const uint32_t b0 = threadIdx.x * per;
-    const uint32_t *tot = P.seg_tot + (size_t)g * bins;
-    uint32_t mine = 0;
-    for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += tot[b];
-    uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
-    run += P.seg_begin ? P.seg_begin[g] : 0;
-    for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
-        P.part_begin[(size_t)g * bins + b] = run;
-        run += tot[b];
-        P.part_end[(size_t)g * bins + b] = run;
-    }
-}
-
-// Grid: one block per bucket. Write cursor of every (unit, bucket).
-__global__ void __launch_bounds__(PLAN_THREADS) unit_scan_kernel(PassParams P) {
-    extern __shared__ uint32_t s_excl[];  // [unit_count]
-    __shared__ uint32_t s_warp[32];
-    const uint32_t b = blockIdx.x;
-    const uint32_t bins = 1u << P.bits;
-    const uint32_t U = *P.unit_count;
-    const uint32_t per = (U + PLAN_THREADS - 1) / PLAN_THREADS;
-    const uint32_t u0 = threadIdx.x * per;
-    uint32_t mine = 0;
-    for (uint32_t u = u0; u < u0 + per && u < U; u++) mine += P.cnt[(size_t)u * bins + b];
-    uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
-    for (uint32_t u = u0; u < u0 + per && u < U; u++) {
-        s_excl[u] = run;
-        run += P.cnt[(size_t)u * bins + b];
-    }
+    __threadfence();
     __syncthreads();
-    for (uint32_t u = threadIdx.x; u < U; u += PLAN_THREADS) {
-        const uint32_t g = P.units[u].x;
-        P.unit_off[(size_t)u * bins + b] = P.part_begin[(size_t)g * bins + b] + s_excl[u] - s_excl[P.seg_first_unit[g]];
+    if (threadIdx.x == 0) s_last = atomicAdd(&P.seg_done[U.g], 1u) + 1 == seg_units(P, U.g);
+    __syncthreads();
+    // ---- the segment's last unit counted: partition bounds of the segment
+    if (s_last) {
+        __threadfence();
+        const uint32_t *tot = P.seg_tot + (size_t)U.g * bins;
+        const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
+        const uint32_t b0 = threadIdx.x * per;
+        uint32_t mine = 0;
+        for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += __ldcg(tot + b);
+        uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
+        run += P.seg_begin ? P.seg_begin[U.g] : 0;
+        for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
+            P.part_begin[(size_t)U.g * bins + b] = run;
+            run += __ldcg(tot + b);
+            P.part_end[(size_t)U.g * bins + b] = run;
+        }
+    }
+
+    // ---- the last unit of all: the next pass's plan over this pass's partitions
+    if (P.next_plan) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(&P.ctl[0], 1u) + 1 == total;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            plan_block(P.part_begin, P.part_end, (uint32_t)(P.nsides * P.Q) * bins, (uint32_t)P.next_max_units, P.min_unit_rows, P.next_plan);
+        }
     }
 }
 
 // Shared memory of the scatter kernel: two input tiles filled by bulk copies, the
-// bucket-sorted output tile (row-contiguous), bucket ids and counters.
+// bucket-sorted output tile (row-contiguous), each sorted row's bucket, and per bucket the
+// tile's counts (two tiles), its start in the sorted tile and the unit's write cursor.
 template <int KW, int PB, int HS, bool IN_AOS, int ITEMS>
 struct ScatterSmem {
     using L = Layout<KW, PB, HS>;
     static constexpr int T = PART_THREADS * ITEMS;
     static constexpr size_t IN_BUF = Chunk<KW, PB, HS, IN_AOS>::bytes(T);
     static constexpr size_t OUT = (size_t)T * (L::STRIDE + 4);  // rows + bucket word per row
-    static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 3 * 4; }
+    // + per bucket: counts of two tiles, start, cursor; chunk totals past 1024 buckets
+    static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 4 * 4 + (bins > 1024 ? bins / 32 * 4 : 0); }
 };
 
 // Rows per thread of a scatter tile: the largest of 4, 2, 1 whose block (with 2^9 bins)
-// stays within about half of an SM's shared memory, so two blocks fit per SM (wider
-// passes, up to 2^12 bins, stay below the 227 KB block limit with one block per SM).
+// fits twice in an SM's 228 KB with the per-block 1 KB reservation and ~0.1 KB of static
+// shared memory (wider passes, up to 2^12 bins, run one block per SM).
+constexpr size_t SCATTER_HALF_SM = 228 * 1024 / 2 - 1024 - 128;
 template <int KW, int PB, int HS, bool IN_AOS>
 constexpr int scatter_items() {
-    return ScatterSmem<KW, PB, HS, IN_AOS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 4>::OUT + 16 + 512 * 12 <= 113 * 1024   ? 4
-           : ScatterSmem<KW, PB, HS, IN_AOS, 2>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 2>::OUT + 16 + 512 * 12 <= 113 * 1024 ? 2
-                                                                                                                                   : 1;
+    return ScatterSmem<KW, PB, HS, IN_AOS, 4>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 4>::OUT + 16 + 512 * 16 <= SCATTER_HALF_SM   ? 4
+           : ScatterSmem<KW, PB, HS, IN_AOS, 2>::IN_BUF * 2 + ScatterSmem<KW, PB, HS, IN_AOS, 2>::OUT + 16 + 512 * 16 <= SCATTER_HALF_SM ? 2
+                                                                                                                                     : 1;
+}
+
+// Tile descriptor passed from the issuing thread to the block: unit, rows [a, b),
+// segment | side << 30 | (first tile of its unit) << 31, and the unit's index in its
+// segment. unit ~0: no tile (end).
+struct TileDesc {
+    uint32_t unit, a, b, gs, rank;
+};
+
+// State of the scatter's issuing thread: the unit it is cutting into tiles.
+struct TileIssuer {
+    uint32_t u = 0, a = 0, e = 0, g = 0, side = 0, rank = 0;
+    bool fresh = false;
+};
+
+// Rows of bucket b in the units of u's segment before u (u is the rank-th unit of its
+// segment), by decoupled look-back over the units' words, LB at a time; then u's own word
+// becomes its inclusive prefix for the units after it. The histogram wrote every unit's
+// count before the scatter started, so no word is ever missing: a walk never waits.
+__device__ __forceinline__ unsigned long long look_back(const PassParams &P, uint32_t u, uint32_t rank, uint32_t b, uint32_t bins) {
+    constexpr uint32_t LB = 4;
+    unsigned long long *mine = P.look + (size_t)u * bins + b;
+    unsigned long long prefix = 0;
+    if (rank > 0) {
+        const unsigned long long own = ld_relaxed(mine);
+        uint32_t left = rank;  // predecessors in the segment not yet added
+        uint32_t v = u - 1;
+        bool done = false;
+        while (!done && left) {
+            const uint32_t n = left < LB ? left : LB;
+            unsigned long long w[LB];
+#pragma unroll
+            for (uint32_t i = 0; i < LB; i++) w[i] = i < n ? ld_relaxed(P.look + (size_t)(v - i) * bins + b) : 0ull;
+#pragma unroll
+            for (uint32_t i = 0; i < LB; i++) {
+                if (done || i >= n) continue;
+                prefix += w[i] & LB_VALUE;
+                done = (w[i] >> 62) == LB_INC;
+            }
+            v -= n;
+            left -= n;
+        }
+        st_relaxed(mine, lb_pack(LB_INC, prefix + (own & LB_VALUE)));
+    }
+    return prefix;
+}
+
+// The same, out of line: for buckets past the block's threads (passes of more than 2^9
+// buckets), whose look-back happens while a tile's ranks are held in registers.
+static __device__ __noinline__ unsigned long long look_back_far(const PassParams &P, uint32_t u, uint32_t rank, uint32_t b, uint32_t bins) { return look_back(P, u, rank, b, bins); }
+
+// Issuing thread of the scatter: the next tile of its current unit, or the first tile of
+// the next unit taken by ticket. Units without rows are skipped; their look-back words stay
+// counts of zero, which later walks add and pass.
+template <int KW, int PB, int HS, bool IN_AOS, int T>
+__device__ __forceinline__ void scatter_issue(const PassParams &P, TileIssuer &is, uint32_t total, unsigned char *buf, uint64_t *bar, TileDesc *desc, uint32_t *deltas) {
+    using C = Chunk<KW, PB, HS, IN_AOS>;
+    const uint32_t bins = 1u << P.bits;
+    while (is.a >= is.e) {
+        const uint32_t u = atomicAdd(&P.ctl[1], 1u);
+        if (u >= total) {
+            *desc = TileDesc{~0u, 0, 0, 0, 0};
+            mbar_arrive(bar);
+            return;
+        }
+        const UnitRange U = unit_range(P, u);
+        is.u = u;
+        is.a = U.a;
+        is.e = U.b;
+        is.g = U.g;
+        is.side = U.side;
+        is.rank = U.rank;
+        is.fresh = true;
+        if (U.a < U.b && bins >= 4) {  // bulk prefetches take multiples of 16 bytes
+            bulk_prefetch_l2(P.look + (size_t)u * bins, bins * 8);
+            bulk_prefetch_l2(P.part_begin + (size_t)U.g * bins, bins * 4);
+        }
+    }
+    const uint32_t b = min(is.e, is.a + (uint32_t)T);
+    *desc = TileDesc{is.u, is.a, b, is.g | (is.side << 30) | (is.fresh ? 1u << 31 : 0u), is.rank};
+    const Side &S = P.side[is.side];
+    fence_proxy_async();
+    C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, is.a, b, T, buf, bar, deltas);
+    is.a = b;
+    is.fresh = false;
 }
 
 template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS>
@@ -550,105 +697,142 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     using Pt = typename PayloadType<PB>::T;
     using SM = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS>;
     constexpr int T = SM::T;
-    extern __shared__ __align__(16) unsigned char s_raw[];
+    extern __shared__ __align__(128) unsigned char s_raw[];
     uint64_t *bar = (uint64_t *)s_raw;
     unsigned char *inb0 = s_raw + 16;
     unsigned char *out_rows = inb0 + 2 * SM::IN_BUF;
-    // bucket of each staged row, and in the high half the next pass's bucket (bid_out)
+    // bucket of each sorted row, and in the high half the next pass's bucket (bid_out)
     uint32_t *st_b = (uint32_t *)(out_rows + (size_t)T * L::STRIDE);
     const uint32_t bins = 1u << P.bits;
-    uint32_t *s_run = (uint32_t *)(st_b + T);
-    uint32_t *s_cnt = s_run + bins;
-    uint32_t *s_start = s_cnt + bins;
-    __shared__ uint32_t s_warp[32];
+    uint32_t *s_cnt = st_b + T;            // [2][bins]: counts of the tile (by parity)
+    uint32_t *s_start = s_cnt + 2 * bins;  // [bins]: bucket start in the sorted tile
+    uint32_t *s_run = s_start + bins;      // [bins]: output row of the tile's first row of the bucket
+    uint32_t *s_chunk = s_run + bins;      // [bins / 32]: chunk totals (more than 1024 buckets)
+    __shared__ TileDesc s_tile[2];
     __shared__ uint32_t s_delta[2][3];
-
-    const uint32_t u = blockIdx.x;
-    if (u >= *P.unit_count) return;
-    const uint4 U = P.units[u];
-    const Side &S = P.side[U.w];
+    const uint32_t total = plan_total(P);
     const uint64_t mask = bins - 1;
-    const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
-    const uint32_t b0 = threadIdx.x * per;
-    const uint32_t ntiles = (U.z - U.y + T - 1) / T;
+    const uint64_t nmask = (1ull << P.next_bits) - 1;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr uint32_t NW = PART_THREADS / 32;
+
+    TileIssuer is;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_proxy_async();
     }
-    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_run[b] = P.unit_off[(size_t)u * bins + b];
+    for (uint32_t b = threadIdx.x; b < 2 * bins; b += PART_THREADS) s_cnt[b] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (uint32_t k = 0; k < 2 && k < ntiles; k++) {
-            const uint32_t a = U.y + k * T;
-            C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T), T, inb0 + k * SM::IN_BUF, &bar[k], s_delta[k]);
-        }
+        scatter_issue<KW, PB, HS, IN_AOS, T>(P, is, total, inb0, &bar[0], &s_tile[0], s_delta[0]);
+        scatter_issue<KW, PB, HS, IN_AOS, T>(P, is, total, inb0 + SM::IN_BUF, &bar[1], &s_tile[1], s_delta[1]);
     }
 
-    if (threadIdx.x == 0 && ntiles > 2) {
-        const uint32_t a = U.y + 2 * T;
-        C::prefetch(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T));
-    }
-    for (uint32_t k = 0; k < ntiles; k++) {
+    for (uint32_t k = 0;; k++) {
         const uint32_t buf = k & 1;
-        const uint32_t tile = U.y + k * T;
-        const uint32_t nt = min(U.z - tile, (uint32_t)T);
-        if (threadIdx.x == 0 && k + 3 < ntiles) {
-            // tile k + 2 is copied once tile k is sorted; have L2 fetch tile k + 3 already
-            const uint32_t a = U.y + (k + 3) * T;
-            C::prefetch(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T));
+        uint32_t *cnt = s_cnt + buf * bins;
+        uint32_t *cnt_prev = s_cnt + (buf ^ 1) * bins;
+        const bool ok = mbar_wait(&bar[buf], (k >> 1) & 1);
+        const TileDesc D = s_tile[buf];
+        const bool end = D.unit == ~0u;
+        const Side &S = P.side[(D.gs >> 30) & 1];
+        const uint32_t nt = D.b - D.a;
+        const bool fresh = (D.gs >> 31) != 0;
+        // a unit's first tile: this thread's first bucket's cursor by look-back, before the
+        // ranks below are live (the other buckets', past the block's threads, in the scan)
+        uint32_t lb0 = 0;
+        if (ok && !end && fresh && threadIdx.x < bins) lb0 = (uint32_t)look_back(P, D.unit, D.rank, threadIdx.x, bins);
+        uint32_t bk[ITEMS], rk[ITEMS];  // bucket | next pass's bucket << 16, rank in the tile
+        const C in = C::view(inb0 + buf * SM::IN_BUF, T, s_delta[buf]);
+        if (ok && !end) {
+#pragma unroll
+            for (int j = 0; j < ITEMS; j++) {
+                const uint32_t i = j * PART_THREADS + threadIdx.x;
+                if (i < nt) {
+                    const uint64_t mh = bucket_hash(in.h_of(i, P.hs), P.hs);
+                    const uint32_t b = (uint32_t)((mh >> P.shift) & mask);
+                    bk[j] = b | (OUT_AOS ? (uint32_t)((mh >> P.next_shift) & nmask) << 16 : 0u);
+                    rk[j] = atomicAdd(&cnt[b], 1u);
+                }
+            }
         }
-        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_cnt[b] = 0;
-        if (!block_wait(&bar[buf], (k >> 1) & 1)) {
+        if (__syncthreads_or(!ok)) {
+            // a bulk copy never landed: flag it, let the other buffer's copy land, leave
             if (threadIdx.x == 0) {
                 atomicOr(P.error, 4u);
-                // let the other copy of this block land before leaving
-                if (k + 1 < ntiles) mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
+                mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
             }
             return;
         }
-        const C in = C::view(inb0 + buf * SM::IN_BUF, T, s_delta[buf]);
-        uint32_t bk[ITEMS];
-        uint32_t rk[ITEMS];
-        uint32_t nb[ITEMS];
-        const uint64_t nmask = (1ull << P.next_bits) - 1;
+        if (end) break;
+
+        // ---- per bucket: the unit's cursor (look-back for a unit's first tile, else the
+        // previous tile's counts added), the previous tile's counts cleared, the start of the
+        // bucket's rows in the sorted tile
+        const uint32_t g = D.gs & 0x3fffffffu;
+        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
+            if (fresh) s_run[b] = P.part_begin[(size_t)g * bins + b] + (b == threadIdx.x ? lb0 : (uint32_t)look_back_far(P, D.unit, D.rank, b, bins));
+            else s_run[b] += cnt_prev[b];
+            cnt_prev[b] = 0;
+        }
+        if (bins <= 1024) {
+            // each warp adds up the buckets before its chunk itself: no barrier
+            for (uint32_t c = warp; c * 32 < bins; c += NW) {
+                const uint32_t b = c * 32 + lane;
+                const uint32_t v = b < bins ? cnt[b] : 0u;
+                uint32_t x = v;
 #pragma unroll
-        for (int j = 0; j < ITEMS; j++) {
-            const uint32_t i = j * PART_THREADS + threadIdx.x;
-            nb[j] = 0;
-            if (i < nt) {
-                const uint64_t mh = bucket_hash(in.h_of(i, P.hs), P.hs);
-                bk[j] = (uint32_t)((mh >> P.shift) & mask);
-                if (OUT_AOS) nb[j] = (uint32_t)((mh >> P.next_shift) & nmask);
-                rk[j] = atomicAdd(&s_cnt[bk[j]], 1u);
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                    if ((int)lane >= o) x += y;
+                }
+                uint32_t s = 0;
+                for (uint32_t i = lane; i < c * 32; i += 32) s += cnt[i];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (b < bins) s_start[b] = s + x - v;
+            }
+        } else {
+            // chunk totals first (one more barrier)
+            const uint32_t nchunks = bins / 32;
+            for (uint32_t c = warp; c < nchunks; c += NW) {
+                uint32_t v = cnt[c * 32 + lane];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) s_chunk[c] = v;
+            }
+            __syncthreads();
+            for (uint32_t c = warp; c < nchunks; c += NW) {
+                const uint32_t b = c * 32 + lane;
+                const uint32_t v = cnt[b];
+                uint32_t x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                    if ((int)lane >= o) x += y;
+                }
+                uint32_t s = 0;
+                for (uint32_t i = lane; i < c; i += 32) s += s_chunk[i];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                s_start[b] = s + x - v;
             }
         }
         __syncthreads();
-        {
-            uint32_t mine = 0;
-            for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += s_cnt[b];
-            uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
-            for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
-                s_start[b] = run;
-                run += s_cnt[b];
-            }
-        }
-        __syncthreads();
+        // ---- rows into bucket order
 #pragma unroll
         for (int j = 0; j < ITEMS; j++) {
             const uint32_t i = j * PART_THREADS + threadIdx.x;
             if (i < nt) {
-                const uint32_t pos = s_start[bk[j]] + rk[j];
+                const uint32_t pos = s_start[bk[j] & 0xffffu] + rk[j];
                 in.copy_row(i, out_rows + (size_t)pos * L::STRIDE);
-                st_b[pos] = bk[j] | (nb[j] << 16);
+                st_b[pos] = bk[j];
             }
         }
-        __syncthreads();  // input buffer `buf` is free: refill it with tile k + 2
-        if (threadIdx.x == 0 && k + 2 < ntiles) {
-            fence_proxy_async();
-            const uint32_t a = U.y + (k + 2) * T;
-            C::issue(S.keys_in, S.pay_in, S.hash_in, S.rows_in, a, min(U.z, a + T), T, inb0 + buf * SM::IN_BUF, &bar[buf], s_delta[buf]);
-        }
+        __syncthreads();  // input buffer `buf` is free: refill it
+        if (threadIdx.x == 0) scatter_issue<KW, PB, HS, IN_AOS, T>(P, is, total, inb0 + buf * SM::IN_BUF, &bar[buf], &s_tile[buf], s_delta[buf]);
+        // ---- bucket runs out: row i of the sorted tile goes to cursor + (i - bucket start)
         for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
             const uint32_t sbk = st_b[i];
             const uint32_t b = sbk & 0xffffu;
@@ -656,13 +840,13 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
             const unsigned char *row = out_rows + (size_t)i * L::STRIDE;
             if (OUT_AOS) {
                 if (S.bid_out) S.bid_out[dst] = (uint16_t)(sbk >> 16);
-                unsigned char *g = (unsigned char *)S.rows_out + (size_t)dst * L::STRIDE;
+                unsigned char *gp = (unsigned char *)S.rows_out + (size_t)dst * L::STRIDE;
                 if (L::STRIDE % 16 == 0) {
 #pragma unroll
-                    for (int o = 0; o < L::STRIDE; o += 16) *(uint4 *)(g + o) = *(const uint4 *)(row + o);
+                    for (int o = 0; o < L::STRIDE; o += 16) *(uint4 *)(gp + o) = *(const uint4 *)(row + o);
                 } else {
 #pragma unroll
-                    for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(g + o) = *(const uint2 *)(row + o);
+                    for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(gp + o) = *(const uint2 *)(row + o);
                 }
             } else {
                 store_key<KW>(S.keys_out, dst, key_from_smem<KW>(row));
@@ -673,9 +857,6 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
                 }
             }
         }
-        __syncthreads();
-        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_run[b] += s_cnt[b];
-        __syncthreads();
     }
 }
 
@@ -878,20 +1059,26 @@ struct Pair<8> {
 //     claim item k + 1 by ticket, L2-prefetch its build and probe rows
 //   consumers, item k:
 //     wait full[b]; load their first probe rows into registers (in flight during the build)
-//     insert the build rows into table[b] (u32 slots: tag << 16 | row + 1, atomicCAS)
+//     insert the build rows into table[b] (u16 slots: tag << 11 | row, atomicCAS)
 //     named barrier over the consumers: the table is complete (the only block-level wait)
 //     probe: rows straight from global memory, J per thread per round, matches staged per
 //     item in stage[b] (one shared-memory reservation per warp and round)
 //     arrive empty[b]
 //
-// Tables are never cleared: a slot belongs to the current item when its tag equals the
-// item's tag (the use count of the table buffer), so stale slots read as empty. Staged pairs
+// Tables are cleared once every 31 uses: a slot belongs to the current item when its 5-bit
+// tag equals the item's tag (the use count of the table buffer, mod 31, plus 1), so stale
+// slots read as empty. Tables hold up to 2048 build rows at 8 slots per row by default
+// (load <= 1/8): a warp walks as far as its longest probe sequence, and at load 1/2 that
+// is about ten slots for a 32-lane miss. Staged pairs
 // leave with one bulk store per item in the order of an atomic reservation; pairs past the
 // stage's capacity (only when an item has more matches than it holds) are written directly
 // with a per-warp reservation.
 
 constexpr int PROBE_THREADS = 1024;
-constexpr int PROBE_J = 4;  // probe rows per consumer thread per round
+constexpr int PROBE_J = 5;  // probe rows per consumer thread per round (4960 per block)
+constexpr uint32_t TAG_SHIFT = 11;  // table slot: tag << TAG_SHIFT | build row (rows < 2048)
+constexpr uint32_t ROW_MASK = (1u << TAG_SHIFT) - 1;
+constexpr uint32_t TAGS = 31;        // tags 1..31
 
 template <int KW, int PB, int HS>
 struct ProbeRow {
@@ -969,7 +1156,7 @@ struct ProbeSmem {
     using PT = typename Pair<PB>::T;
     __host__ __device__ static size_t rbuf_bytes(uint32_t rcap) { return (C::bytes(rcap) + 127) / 128 * 128; }
     __host__ __device__ static size_t bytes(uint32_t rcap, uint32_t tcap, uint32_t scap) {
-        return 128 + 2 * rbuf_bytes(rcap) + 2 * (size_t)tcap * 4 + 2 * (size_t)scap * sizeof(PT);
+        return 128 + 2 * rbuf_bytes(rcap) + 2 * (size_t)tcap * 2 + 2 * (size_t)scap * sizeof(PT);
     }
 };
 
@@ -1039,7 +1226,7 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
     uint64_t *empty = full + 2;          // [2]: consumers done with the item
     const size_t rbytes = SM::rbuf_bytes(Q.rcap);
     unsigned char *rbuf0 = s_raw + 128;
-    uint32_t *tab0 = (uint32_t *)(rbuf0 + 2 * rbytes);
+    uint16_t *tab0 = (uint16_t *)(rbuf0 + 2 * rbytes);
     PT *stage0 = (PT *)(tab0 + 2 * (size_t)Q.tcap);
     __shared__ uint4 s_desc[2];
     __shared__ uint32_t s_item[2], s_join[2], s_dups[2], s_out_n[2];
@@ -1059,7 +1246,7 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
         s_dups[0] = s_dups[1] = 0;
         fence_proxy_async();
     }
-    for (uint32_t i = threadIdx.x; i < 2 * Q.tcap; i += blockDim.x) tab0[i] = 0;
+    for (uint32_t i = threadIdx.x; i < 2 * Q.tcap / 8; i += blockDim.x) ((uint4 *)tab0)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
 
     if (warp == NC / 32) {
@@ -1143,12 +1330,12 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
         const uint32_t item = got ? s_item[b] : 0xffffffffu;
         const bool stop = !got || item >= total;
         const uint32_t use = k >> 1;                  // uses of table b before this one
-        const uint32_t tag = use % 65535u + 1u;       // 1..65535
-        uint32_t *T = tab0 + (size_t)b * Q.tcap;
-        if (use > 0 && use % 65535u == 0) {
+        const uint32_t tag = use % TAGS + 1u;         // 1..31
+        uint16_t *T = tab0 + (size_t)b * Q.tcap;
+        if (use > 0 && use % TAGS == 0) {
             // the tag wraps: clear the table (its last item finished before the previous
             // item's table barrier)
-            for (uint32_t i = c; i < Q.tcap; i += NC) T[i] = 0;
+            for (uint32_t i = c; i < Q.tcap / 8; i += NC) ((uint4 *)T)[i] = make_uint4(0, 0, 0, 0);
             bar_sync(1, NC);
         }
         uint4 d = make_uint4(0, 0, 0, 0);
@@ -1168,23 +1355,23 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
         while (cap < nr * Q.tmul && cap < Q.tcap) cap <<= 1;
         const uint32_t cmask = cap - 1;
         const C R = C::view(rbuf0 + b * rbytes, Q.rcap, s_rdelta[b]);
-        // ---- build: slot = tag << 16 | (row + 1); an equal key met on the way marks the item
-        // as having duplicate build keys
+        // ---- build: slot = tag << 11 | row; an equal key met on the way marks the item as
+        // having duplicate build keys
         bool dup = false;
         for (uint32_t i = c; i < nr; i += NC) {
             const Key<KW> key = R.key(i);
             const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
             uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
-            const uint32_t val = (tag << 16) | (i + 1);
+            const unsigned short val = (unsigned short)((tag << TAG_SHIFT) | i);
             uint32_t cur = T[slot];
             for (uint32_t tries = 0;;) {
-                if ((cur >> 16) != tag) {
-                    const uint32_t prev = atomicCAS(&T[slot], cur, val);
+                if ((cur >> TAG_SHIFT) != tag) {
+                    const uint32_t prev = atomicCAS((unsigned short *)&T[slot], (unsigned short)cur, val);
                     if (prev == cur) break;
                     cur = prev;
                     continue;
                 }
-                dup |= key_equal<KW>(R.key((cur & 0xffffu) - 1), key);
+                dup |= key_equal<KW>(R.key(cur & ROW_MASK), key);
                 if (++tries > cap) {  // cannot happen: at most 1/tmul of the slots are used
                     atomicOr(Q.error, 1u);
                     break;
@@ -1227,8 +1414,8 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
                         uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
                         for (uint32_t t = 0; t < cap; t++) {
                             const uint32_t e = T[slot];
-                            if ((e >> 16) != tag) break;
-                            const uint32_t bi = (e & 0xffffu) - 1;
+                            if ((e >> TAG_SHIFT) != tag) break;
+                            const uint32_t bi = e & ROW_MASK;
                             if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == h)) {
                                 m[j] = (int)bi;
                                 break;
@@ -1271,10 +1458,10 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
                         Pt rp = 0;
                         if (active) {
                             const uint32_t e = T[slot];
-                            if ((e >> 16) != tag || ++steps > cap) {
+                            if ((e >> TAG_SHIFT) != tag || ++steps > cap) {
                                 active = false;
                             } else {
-                                const uint32_t bi = (e & 0xffffu) - 1;
+                                const uint32_t bi = e & ROW_MASK;
                                 if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == h)) {
                                     match = true;
                                     rp = R.pay(bi);
