@@ -283,13 +283,17 @@ VJ_API int vj_result_free(vj_ctx *ctx, vj_result *result);
  * Autotuner. The reference sweeps its tunables (bucket counts, vector sizes, kernel shapes)
  * from TOML grids in separate benchmark runs (src/benchmark/configuration.hpp:200-305).
  * vj_tune runs candidate plans of a join of r and s on this context -- the planner's
- * choice, two passes with the bits split both ways around the total that fills the
- * shared-memory tables (and one bit more or less), one pass, L2-resident tables for large
- * build sides; at most max_candidates (0 = 12) -- each a full join into d_pairs (capacity
+ * choice, the same with fuller tables (load <= 1/4, 1/2) and with 512-thread probe blocks,
+ * two passes with the bits split both ways around the total that fills the shared-memory
+ * tables (and one bit more or less), one pass; at most max_candidates (0 = 16) -- each a
+ * full join into d_pairs (capacity
  * pairs), and keeps the fastest for the join's shape class (key words, payload bytes,
  * ceil(log2 |R|), ceil(log2 |S|), hash algorithm and width of `base`). Later vj_join calls
  * on this context with automatic options (NULL or all fields zero but the hash) of that
- * class use it. *best / *best_ms (optional) receive the winner and its time.
+ * class use it, and so do vj_join_host, vj_join_batch (for the class of its largest join:
+ * max_build_rows build rows, probe rows in the batch's ratio) and the slots of a server
+ * the cache is shared with (vj_server_share_tuning). *best / *best_ms (optional) receive
+ * the winner and its time.
  * vj_tune_save / vj_tune_load write / merge the context's cache as a text file.
  */
 VJ_API int vj_tune(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *base, void *d_pairs, uint64_t capacity, int max_candidates, vj_join_options *best, float *best_ms,
@@ -345,6 +349,9 @@ typedef struct vj_request_result {
     double submit_s;    /* submitted, started, finished: seconds since the server started */
     double start_s;
     double finish_s;
+    int32_t passes;     /* the plan the join ran: radix passes, their bits, build rows per table */
+    int32_t radix_bits[2];
+    uint32_t build_rows;
 } vj_request_result;
 typedef struct vj_server_stats {
     uint64_t submitted;
@@ -358,6 +365,10 @@ VJ_API int vj_server_create(int device, uint64_t memory_budget_bytes, int slots,
 VJ_API int vj_server_submit(vj_server *srv, const vj_table *r, const vj_table *s, const vj_join_options *options, void *d_pairs, uint64_t capacity, uint64_t *request_id);
 VJ_API int vj_server_wait(vj_server *srv, uint64_t request_id, vj_request_result *out);
 VJ_API int vj_server_stats_get(vj_server *srv, vj_server_stats *out);
+/* Copies the tuning cache of ctx (vj_tune results, vj_tune_load entries) into every slot:
+ * requests with automatic options then run the tuned plan of their shape class. Call it
+ * while no request is queued or running (VJ_ERR_INVALID_ARGUMENT otherwise). */
+VJ_API int vj_server_share_tuning(vj_server *srv, const vj_ctx *ctx);
 VJ_API int vj_server_destroy(vj_server *srv);
 
 /* Order-independent digest of a pair list: sum and xor of a 64-bit mix of each pair, the

@@ -926,6 +926,17 @@ int batch_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_
     ctx->profiling = prof;
     VJ_TRY(st);
     if (d_status) VJ_CUDA(cudaMemcpyAsync(d_status, run.d_error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+    // the plan the batch ran (no stage times: nothing synchronises)
+    vj_profile &p = ctx->last;
+    memset(&p, 0, sizeof(p));
+    p.passes = pl.passes;
+    p.kernel_launches = ctx->launches;
+    p.radix_bits[0] = pl.bits[0];
+    p.radix_bits[1] = pl.bits[1];
+    p.build_rows = pl.rcap;
+    p.probe_rows = pl.schunk;
+    p.rows[0] = t.rows[0];
+    p.rows[1] = t.rows[1];
     return VJ_OK;
 }
 
@@ -1012,6 +1023,12 @@ extern "C" int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, 
     call.hs = spec_from(options, 1);
     call.opt = options;
     call.max_build_rows = max_build_rows && max_build_rows < r->rows ? max_build_rows : r->rows;
+    // a tuned plan for the class of the batch's largest join, if any (probe rows in the
+    // batch's ratio)
+    vj_table rmax = *r, smax = *s;
+    rmax.rows = call.max_build_rows;
+    smax.rows = (uint64_t)((double)call.max_build_rows * ((double)s->rows / (double)r->rows)) + 1;
+    call.opt = tuned_options(ctx, &rmax, &smax, options);
     call.pairs = d_pairs;
     call.status = d_status;
     call.stream = st;

@@ -148,6 +148,10 @@ struct vj_server {
             lock.lock();
             r->res.status = st;
             r->res.count = out.count;
+            r->res.passes = sl.ctx->last.passes;
+            r->res.radix_bits[0] = sl.ctx->last.radix_bits[0];
+            r->res.radix_bits[1] = sl.ctx->last.radix_bits[1];
+            r->res.build_rows = sl.ctx->last.build_rows;
             r->res.finish_s = fin;
             r->done = true;
             sl.busy = false;
@@ -233,6 +237,15 @@ extern "C" int vj_server_wait(vj_server *srv, uint64_t request_id, vj_request_re
     *out = q->res;
     srv->requests.erase(request_id);  // the iterator may be stale after the wait
     delete q;
+    return VJ_OK;
+}
+
+extern "C" int vj_server_share_tuning(vj_server *srv, const vj_ctx *ctx) {
+    using namespace vj;
+    VJ_CHECK(srv && ctx, VJ_ERR_INVALID_ARGUMENT, "vj_server_share_tuning: null argument");
+    std::lock_guard<std::mutex> lock(srv->mu);
+    VJ_CHECK(srv->queue.empty() && srv->stats.completed == srv->stats.submitted, VJ_ERR_INVALID_ARGUMENT, "vj_server_share_tuning: requests are queued or running");
+    for (auto &sl : srv->slots) sl.ctx->tuned = ctx->tuned;
     return VJ_OK;
 }
 

@@ -5,10 +5,11 @@
 // runs (src/benchmark/configuration.hpp:200-305: bucket counts, vector sizes, kernel
 // shapes); here the sweep runs on the caller's own tables, inside the library.
 //
-// Candidates: the planner's own choice; two passes with the bits split both ways around
-// the total that fills shared-memory tables, and one bit more or less (with build tables
-// sized to match); one pass where the total fits one pass; L2-resident tables after one
-// pass of 9 or 10 bits for large build sides.
+// Candidates: the planner's own choice; the same with a fuller table (load <= 1/4, 1/2)
+// and with a smaller probe block (512 threads: one producer warp, 15 consumers); two
+// passes with the bits split both ways around the total that fills shared-memory tables,
+// and one bit more or less (with build tables sized to match); one pass where the total
+// fits one pass.
 #include "vj_internal.cuh"
 
 #include <cmath>
@@ -27,7 +28,8 @@ int lg(uint64_t x) {
 
 bool automatic(const vj_join_options *o) {
     if (!o) return true;
-    return o->flags == 0 && o->passes == 0 && o->radix_bits[0] == 0 && o->radix_bits[1] == 0 && o->build_rows == 0 && o->probe_rows == 0 && o->probe_threads == 0 && o->probe_sub_rows == 0;
+    return o->flags == 0 && o->passes == 0 && o->radix_bits[0] == 0 && o->radix_bits[1] == 0 && o->build_rows == 0 && o->probe_rows == 0 && o->probe_threads == 0 && o->probe_sub_rows == 0 &&
+           o->table_load_pct == 0;
 }
 
 vj_join_options base_of(const vj_join_options *b) {
@@ -44,6 +46,16 @@ std::vector<vj_join_options> candidates(const vj_table *r, const vj_join_options
     std::vector<vj_join_options> c;
     const vj_join_options b = base_of(base);
     c.push_back(b);  // the planner's own choice
+    for (int load : {25, 50}) {  // block shape and table load of the planner's plan
+        vj_join_options o = b;
+        o.table_load_pct = load;
+        c.push_back(o);
+    }
+    {
+        vj_join_options o = b;
+        o.probe_threads = 512;
+        c.push_back(o);
+    }
     const int lr = lg(r->rows);
     const int total = lr > 10 ? lr - 10 : 0;  // partitions of ~1024 build rows: half a 2048-row table
     for (int t = total - 1; t <= total + 1; t++) {
@@ -114,7 +126,7 @@ extern "C" int vj_tune(vj_ctx *ctx, const vj_table *r, const vj_table *s, const 
     cudaEvent_t e0, e1;
     VJ_CUDA(cudaEventCreate(&e0));
     VJ_CUDA(cudaEventCreate(&e1));
-    const std::vector<vj_join_options> cand = candidates(r, base, max_candidates > 0 ? max_candidates : 12);
+    const std::vector<vj_join_options> cand = candidates(r, base, max_candidates > 0 ? max_candidates : 16);
     float top = INFINITY;
     vj_join_options win = cand[0];
     uint64_t first_count = UINT64_MAX;
@@ -170,11 +182,11 @@ extern "C" int vj_tune_save(const vj_ctx *ctx, const char *path) {
     VJ_CHECK(ctx && path, VJ_ERR_INVALID_ARGUMENT, "vj_tune_save: null argument");
     FILE *f = fopen(path, "w");
     VJ_CHECK(f != nullptr, VJ_ERR_INVALID_ARGUMENT, "vj_tune_save: cannot write %s", path);
-    fprintf(f, "# vj tuning cache: kw pb lg_r lg_s algo hash_bits | flags passes bits0 bits1 build_rows probe_rows threads sub_rows | ms\n");
+    fprintf(f, "# vj tuning cache: kw pb lg_r lg_s algo hash_bits | flags passes bits0 bits1 build_rows probe_rows threads table_load_pct | ms\n");
     for (const TuneEntry &e : ctx->tuned) {
         const vj_join_options &o = e.opt;
         fprintf(f, "%d %d %d %d %d %d | %d %d %d %d %d %d %d %d | %.4f\n", e.key.kw, e.key.pb, e.key.lg_r, e.key.lg_s, e.key.algo, e.key.hash_bits, o.flags, o.passes, o.radix_bits[0], o.radix_bits[1], o.build_rows,
-                o.probe_rows, o.probe_threads, o.probe_sub_rows, e.ms);
+                o.probe_rows, o.probe_threads, o.table_load_pct, e.ms);
     }
     const bool ok = fclose(f) == 0;
     VJ_CHECK(ok, VJ_ERR_INVALID_ARGUMENT, "vj_tune_save: cannot write %s", path);
@@ -194,7 +206,7 @@ extern "C" int vj_tune_load(vj_ctx *ctx, const char *path) {
         memset(&e, 0, sizeof(e));
         vj_join_options &o = e.opt;
         const int n = sscanf(line, "%d %d %d %d %d %d | %d %d %d %d %d %d %d %d | %f", &e.key.kw, &e.key.pb, &e.key.lg_r, &e.key.lg_s, &e.key.algo, &e.key.hash_bits, &o.flags, &o.passes, &o.radix_bits[0],
-                             &o.radix_bits[1], &o.build_rows, &o.probe_rows, &o.probe_threads, &o.probe_sub_rows, &e.ms);
+                             &o.radix_bits[1], &o.build_rows, &o.probe_rows, &o.probe_threads, &o.table_load_pct, &e.ms);
         if (n != 15 || e.key.algo < 0 || e.key.algo >= VJ_HASH_COUNT || (e.key.hash_bits != 32 && e.key.hash_bits != 64)) {
             fclose(f);
             return set_error(VJ_ERR_INVALID_ARGUMENT, "vj_tune_load: %s line %d is not a tuning entry", path, lineno);

@@ -69,6 +69,7 @@ EXPORTS = [
     "vj_server_wait",
     "vj_server_stats_get",
     "vj_server_destroy",
+    "vj_server_share_tuning",
     "vj_join_host",
     "vj_result_free",
     "vj_pairs_digest",
@@ -170,6 +171,9 @@ class VjRequestResult(ctypes.Structure):
         ("submit_s", ctypes.c_double),
         ("start_s", ctypes.c_double),
         ("finish_s", ctypes.c_double),
+        ("passes", ctypes.c_int32),
+        ("radix_bits", ctypes.c_int32 * 2),
+        ("build_rows", ctypes.c_uint32),
     ]
 
 
@@ -246,6 +250,8 @@ def load() -> ctypes.CDLL:
         L.vj_server_wait.argtypes = [vp, u64, ctypes.POINTER(VjRequestResult)]
         L.vj_server_stats_get.restype = i32
         L.vj_server_stats_get.argtypes = [vp, ctypes.POINTER(VjServerStats)]
+        L.vj_server_share_tuning.restype = i32
+        L.vj_server_share_tuning.argtypes = [vp, vp]
         L.vj_server_destroy.restype = i32
         L.vj_server_destroy.argtypes = [vp]
         L.vj_tune.restype = i32
@@ -499,6 +505,10 @@ class Server:
         check(self.lib.vj_server_wait(self.handle, rid, ctypes.byref(res)))
         self._keep.pop(rid, None)
         return res
+
+    def share_tuning(self, ctx: "Context") -> None:
+        """vj_server_share_tuning: the slots use ctx's tuning cache."""
+        check(self.lib.vj_server_share_tuning(self.handle, ctx.handle))
 
     def stats(self) -> VjServerStats:
         st = VjServerStats()
