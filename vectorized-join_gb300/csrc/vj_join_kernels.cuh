@@ -486,20 +486,22 @@ __device__ __forceinline__ uint64_t global_row_hash(const Side &S, uint32_t i, c
     return row_hash<KW>(load_key_stream<KW>(S.keys_in, i), hs);
 }
 
-// Grid: one block per unit of the plan (blocks past the plan's units leave at once).
+// Grid: one block per unit of the plan (blocks past the plan's units leave at once). Four
+// blocks per SM (32 registers a thread) keep enough loads in flight.
 template <int KW, int PB, int HS, bool AOS>
-__global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
+__global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P) {
     extern __shared__ uint32_t s_hist[];
     __shared__ uint32_t s_last;
     __shared__ uint32_t s_warp[32];
+    __shared__ UnitRange s_unit;  // kept in shared memory: no registers held across the count
     const uint32_t bins = 1u << P.bits;
     const uint64_t mask = bins - 1;
     const uint32_t u = blockIdx.x;
-    const uint32_t total = plan_total(P);
-    if (u >= total) return;
+    if (u >= plan_total(P)) return;
+    if (threadIdx.x == 0) s_unit = unit_range(P, u);
     for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
     __syncthreads();
-    const UnitRange U = unit_range(P, u);
+    const UnitRange &U = s_unit;
     const Side &S = P.side[U.side];
 
     // ---- count
@@ -547,9 +549,13 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
         L[b] = lb_pack(U.first ? LB_INC : LB_AGG, c);
         if (c) atomicAdd(&P.seg_tot[(size_t)U.g * bins + b], c);
     }
-    __threadfence();
+    // the block's totals are ordered before its count of the segment's units: the barrier
+    // orders them before thread 0, whose fence makes them visible device-wide
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&P.seg_done[U.g], 1u) + 1 == seg_units(P, U.g);
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&P.seg_done[U.g], 1u) + 1 == seg_units(P, U.g);
+    }
     __syncthreads();
     // ---- the segment's last unit counted: partition bounds of the segment
     if (s_last) {
@@ -570,9 +576,11 @@ __global__ void __launch_bounds__(PART_THREADS) histogram_kernel(PassParams P) {
 
     // ---- the last unit of all: the next pass's plan over this pass's partitions
     if (P.next_plan) {
-        __threadfence();
         __syncthreads();
-        if (threadIdx.x == 0) s_last = atomicAdd(&P.ctl[0], 1u) + 1 == total;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&P.ctl[0], 1u) + 1 == plan_total(P);
+        }
         __syncthreads();
         if (s_last) {
             __threadfence();
