@@ -1411,49 +1411,26 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
                 // Unique build keys: a probe row matches at most one build row. Every lane
                 // resolves its J rows, then the warp stages all its matches behind one
                 // shared-memory reservation.
-                // The J rows' first slots and their build keys are read side by side (two
-                // rounds of independent shared-memory loads); only a row whose first slot
-                // holds another key walks on.
                 int m[J];
-                uint32_t slot[J], e[J];
-                uint32_t walk = 0;  // rows whose first slot holds another key
-#pragma unroll
-                for (int j = 0; j < J; j++) {
-                    const uint64_t h = HS ? rows[j].hash : row_hash<KW>(rows[j].key, Q.hs);
-                    slot[j] = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
-                }
-#pragma unroll
-                for (int j = 0; j < J; j++) e[j] = T[slot[j]];
-#pragma unroll
-                for (int j = 0; j < J; j++) {
-                    m[j] = -1;
-                    const bool live = r0 + c + (uint32_t)j * NC < ns && (e[j] >> TAG_SHIFT) == tag;
-                    if (live) {
-                        const uint32_t bi = e[j] & ROW_MASK;
-                        if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == rows[j].hash)) m[j] = (int)bi;
-                        else walk |= 1u << j;
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < J; j++) {
-                    if (walk & (1u << j)) {
-                        uint32_t sl = (slot[j] + 1) & cmask;
-                        for (uint32_t t = 1; t < cap; t++) {
-                            const uint32_t ev = T[sl];
-                            if ((ev >> TAG_SHIFT) != tag) break;
-                            const uint32_t bi = ev & ROW_MASK;
-                            if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == rows[j].hash)) {
-                                m[j] = (int)bi;
-                                break;
-                            }
-                            sl = (sl + 1) & cmask;
-                        }
-                    }
-                }
                 uint32_t bal[J];
                 uint32_t cnt = 0;
 #pragma unroll
                 for (int j = 0; j < J; j++) {
+                    m[j] = -1;
+                    if (r0 + c + (uint32_t)j * NC < ns) {
+                        const uint64_t h = HS ? rows[j].hash : row_hash<KW>(rows[j].key, Q.hs);
+                        uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
+                        for (uint32_t t = 0; t < cap; t++) {
+                            const uint32_t e = T[slot];
+                            if ((e >> TAG_SHIFT) != tag) break;
+                            const uint32_t bi = e & ROW_MASK;
+                            if (key_equal<KW>(R.key(bi), rows[j].key) && (!HS || R.hash(bi) == h)) {
+                                m[j] = (int)bi;
+                                break;
+                            }
+                            slot = (slot + 1) & cmask;
+                        }
+                    }
                     bal[j] = __ballot_sync(0xffffffffu, m[j] >= 0);
                     cnt += __popc(bal[j]);
                 }
