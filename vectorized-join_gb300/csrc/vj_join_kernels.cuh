@@ -257,12 +257,27 @@ struct Chunk {
     __device__ __forceinline__ P pay(uint32_t i) const { return *(const P *)(p + (size_t)i * (AOS ? L::STRIDE : PB)); }
     __device__ __forceinline__ uint64_t hash(uint32_t i) const { return read_hash<HS>(h + (size_t)i * (AOS ? L::STRIDE : HS)); }
     __device__ __forceinline__ uint64_t h_of(uint32_t i, const HashSpec &hs) const { return HS ? hash(i) : row_hash<KW>(key(i), hs); }
-    // copy of row i as raw bytes into `dst` (row-contiguous layout)
+    // copy of row i as raw bytes into `dst` (row-contiguous layout), one shared-memory
+    // store per row where the row is 8 or 16 bytes: the rows land at random positions, and
+    // a warp's store costs as many passes as lanes hitting one bank group, so two stores of
+    // half rows cost twice the bank conflicts of one. Row-contiguous inputs are the join's
+    // own buffers (256-byte aligned), so their rows are 16-byte aligned when STRIDE is.
     __device__ __forceinline__ void copy_row(uint32_t i, unsigned char *dst) const {
         if (AOS) {
             const unsigned char *src = k + (size_t)i * L::STRIDE;
+            if (L::STRIDE % 16 == 0) {
 #pragma unroll
-            for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(dst + o) = *(const uint2 *)(src + o);
+                for (int o = 0; o < L::STRIDE; o += 16) *(uint4 *)(dst + o) = *(const uint4 *)(src + o);
+            } else {
+#pragma unroll
+                for (int o = 0; o < L::STRIDE; o += 8) *(uint2 *)(dst + o) = *(const uint2 *)(src + o);
+            }
+        } else if (KW == 2 && PB == 8 && HS == 0) {
+            const uint2 kk = *(const uint2 *)(k + (size_t)i * 8);
+            const uint2 pp = *(const uint2 *)(p + (size_t)i * 8);
+            *(uint4 *)dst = make_uint4(kk.x, kk.y, pp.x, pp.y);
+        } else if (KW == 1 && PB == 4 && HS == 0) {
+            *(uint2 *)dst = make_uint2(*(const uint32_t *)(k + (size_t)i * 4), *(const uint32_t *)(p + (size_t)i * 4));
         } else {
             key_to_smem<KW>(dst, key(i));
             *(P *)(dst + L::PAY_OFF) = pay(i);
