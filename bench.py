@@ -436,8 +436,9 @@ def run_skew_join(args) -> None:
 
 def run_batch_join(args) -> None:
     """4096 independent int32 joins, |R_i| log-uniform over [2^10, 2^20], |S_i| = 4 |R_i|,
-    75% of S_i drawn from R_i (per-join seed = 42 + i): one vj_join_batch call replayed from
-    a CUDA graph, against the same 4096 joins as sequential vj_join calls."""
+    75% of S_i drawn from R_i (per-join seed = 42 + i): one vj_join_batch call (one fused,
+    persistent launch) replayed from a CUDA graph, against the same batch as separate
+    launches (VJ_JOIN_BATCH_LAUNCHES) and the same 4096 joins as sequential vj_join calls."""
     import numpy as np
     import torch
 
@@ -473,19 +474,28 @@ def run_batch_join(args) -> None:
     ctx = vj.Context(0)
     t_r, t_s = vj.table(rk, rp, nr, 1, 4), vj.table(sk, sp, ns, 1, 4)
     stream = torch.cuda.Stream()
-    call = lambda: ctx.join_batch(t_r, t_s, joins, d_r, d_s, pairs, d_p, ns, counts, status, max_build_rows=int(r_sizes.max()), stream=stream)
-    call()  # grows the workspace outside the capture
-    torch.cuda.synchronize()
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g, stream=stream):
-        call()
-    g.replay()
-    torch.cuda.synchronize()
-    assert int(status.item()) == 0
-    got = counts.cpu().numpy()
-    for j in range(joins):
-        assert got[j] == want[j][0], j
-        assert vj.pairs_digest(pairs[int(p_off[j]) :], int(got[j]), 4) == (want[j][1], want[j][2]), j
+    def graph_of(opts):
+        call = lambda: ctx.join_batch(t_r, t_s, joins, d_r, d_s, pairs, d_p, ns, counts, status, max_build_rows=int(r_sizes.max()), opts=opts, stream=stream)
+        call()  # grows the workspace outside the capture
+        torch.cuda.synchronize()
+        launches = ctx.last_profile().kernel_launches
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            call()
+        counts.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        got = counts.cpu().numpy()
+        for j in range(joins):
+            assert got[j] == want[j][0], j
+            assert vj.pairs_digest(pairs[int(p_off[j]) :], int(got[j]), 4) == (want[j][1], want[j][2]), j
+        return g, launches
+
+    g_sep, launches_sep = graph_of(vj.options(batch_launches=True))
+    ms_sep = _timed(torch, torch.cuda.current_stream(), g_sep.replay, args.steps, args.warmup)
+    del g_sep
+    g, launches_fused = graph_of(None)
     sampler = ClockSampler(0)
     sampler.start()
     ms = _timed(torch, torch.cuda.current_stream(), g.replay, args.steps, args.warmup)  # replay() launches on the current stream
@@ -522,6 +532,8 @@ def run_batch_join(args) -> None:
     line = _base_line(METRIC, n / (t_batch / 1000), UNIT, args.steps, args.warmup, t_batch, "int32", cfg)
     line["join_roofline"] = {"bytes_alg_per_join": b_alg, "achieved": b_alg / (t_batch / 1000) / 1e9, "peak": peak, "unit": "GB/s", "frac": b_alg / (t_batch / 1000) / 1e9 / peak, "peak_source": src, "passes": 1}
     line["latency_ms"] = _latency(ms)
+    line["gpu_launches"] = launches_fused
+    line["separate_launches"] = {"ms": sum(ms_sep) / len(ms_sep), "value": n / (sum(ms_sep) / len(ms_sep) / 1000), "unit": UNIT, "kernel_launches": launches_sep, "api": "the same vj_join_batch with VJ_JOIN_BATCH_LAUNCHES, in a CUDA graph"}
     line["sequential"] = {"ms": t_seq, "value": n / (t_seq / 1000), "unit": UNIT, "api": "4096 vj_join calls back to back"}
     line["speedup_vs_sequential"] = t_seq / t_batch
     line["matches"] = m

@@ -224,8 +224,10 @@ VJ_API int vj_build_probe(vj_ctx *ctx, const vj_table *r, const void *d_r_hashes
  * on every measured shape, and a join that asks for it returns VJ_ERR_UNSUPPORTED. */
 /* VJ_JOIN_TEST_DEVICE_FLAG is for tests of error reporting: after the probe a kernel sets a
  * flag in the join's device error word, as a kernel whose bounded wait ran out does, and the
- * call returns VJ_ERR_DEVICE. */
-enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4, VJ_JOIN_TEST_DEVICE_FLAG = 1 << 16 };
+ * call returns VJ_ERR_DEVICE. VJ_JOIN_BATCH_LAUNCHES (vj_join_batch only) runs the batch as
+ * its phases' separate kernel launches instead of the one fused, persistent launch (same
+ * results; kept for comparison). */
+enum { VJ_JOIN_FIXED_PASSES = 1, VJ_JOIN_SHARED_TABLES = 2, VJ_JOIN_L2_TABLES = 4, VJ_JOIN_TEST_DEVICE_FLAG = 1 << 16, VJ_JOIN_BATCH_LAUNCHES = 1 << 17 };
 typedef struct vj_join_options {
     int32_t hash_algo;      /* VJ_HASH_*: the hash the partitions are cut from */
     int32_t hash_bits;      /* 32 or 64; 0 = 64 */
@@ -313,10 +315,14 @@ VJ_API int vj_tune_load(vj_ctx *ctx, const char *path);
  * were dropped. max_build_rows: the largest join's build rows (plans the radix pass; 0 =
  * all of r). *d_status (device, optional) receives the kernels' flags: 0 = ok, 16 = an
  * offset was out of range or decreasing and was clamped (that join's results are then
- * unspecified). Asynchronous: no host synchronisation, and once the context's workspace
- * has grown to a batch of this shape, no allocation -- repeated calls can be captured in
- * a CUDA graph after one call outside the capture. Each join's pairs equal vj_join's on
- * the same rows.
+ * unspecified), 64 = a grid-barrier wait of the fused launch ran out (a block could not
+ * run: the results are unspecified). Asynchronous: no host synchronisation, and once the
+ * context's workspace has grown to a batch of this shape, no allocation -- repeated calls
+ * can be captured in a CUDA graph after one call outside the capture. The batch runs as
+ * one persistent, cooperative kernel launch (plus memsets of its counters): the radix pass,
+ * the build tables and the probes of all joins, phase after phase over the whole GPU
+ * (probe_threads is ignored: its blocks are 1024 threads). Each join's pairs equal
+ * vj_join's on the same rows.
  */
 VJ_API int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, uint32_t joins, const uint64_t *d_r_offsets, const uint64_t *d_s_offsets, uint64_t max_build_rows,
                          const vj_join_options *options, void *d_pairs, const uint64_t *d_pair_offsets, uint64_t pair_capacity, uint64_t *d_counts, uint32_t *d_status, vj_stream_t stream);

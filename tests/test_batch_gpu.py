@@ -1,6 +1,8 @@
-"""vj_join_batch: many independent joins in one launch sequence. Every join's pairs must
+"""vj_join_batch: many independent joins in one fused, persistent launch (or, with
+VJ_JOIN_BATCH_LAUNCHES, the same phases as separate launches). Every join's pairs must
 equal the oracle's (small joins) and vj_join's on the same rows (larger ones), in its own
-output range; per-join capacities, out-of-range offsets and CUDA-graph replay included."""
+output range; per-join capacities, out-of-range offsets, CUDA-graph replay and the graph's
+single kernel node included."""
 from __future__ import annotations
 
 import numpy as np
@@ -60,13 +62,16 @@ def run_batch(vjlib, ctx, cuda, rk, rp, sk, sp, r_off, s_off, caps, max_r=0, opt
     return counts.cpu().numpy().view(np.uint64), out, p_off, int(status.cpu().numpy()[0])
 
 
+@pytest.mark.parametrize("launches", [False, True], ids=["fused", "launches"])
 @pytest.mark.parametrize("key_dtype", [np.uint32, np.uint64])
-def test_batch_matches_oracle_per_join(vjlib, ctx, cuda, oracle, key_dtype):
+def test_batch_matches_oracle_per_join(vjlib, ctx, cuda, oracle, key_dtype, launches):
     rng = np.random.default_rng(31 if key_dtype == np.uint32 else 32)
     rk, rp, sk, sp, r_off, s_off = make_batch(rng, 60, 3000, key_dtype)
     wants = oracle_per_join(oracle, rk, rp, sk, sp, r_off, s_off)
     caps = np.array([max(1, w[0]) for w in wants], np.uint64)
-    counts, out, p_off, status = run_batch(vjlib, ctx, cuda, rk, rp, sk, sp, r_off, s_off, caps, max_r=3000)
+    opts = vjlib.options(batch_launches=True) if launches else None
+    counts, out, p_off, status = run_batch(vjlib, ctx, cuda, rk, rp, sk, sp, r_off, s_off, caps, max_r=3000, opts=opts)
+    assert ctx.last_profile().kernel_launches == 1 if not launches else ctx.last_profile().kernel_launches > 1
     assert status == 0
     for j, (cnt, want) in enumerate(wants):
         assert counts[j] == cnt, j
@@ -79,7 +84,8 @@ def test_batch_duplicates_pass_choices(vjlib, ctx, cuda, oracle):
     rk, rp, sk, sp, r_off, s_off = make_batch(rng, 24, 40_000, np.uint64, dup_domain=5000)
     wants = oracle_per_join(oracle, rk, rp, sk, sp, r_off, s_off)
     caps = np.array([max(1, w[0]) for w in wants], np.uint64)
-    for opts in (None, vjlib.options(passes=1, radix_bits=(6, 0)), vjlib.options(passes=0)):
+    variants = (None, vjlib.options(passes=1, radix_bits=(6, 0)), vjlib.options(passes=0), vjlib.options(passes=1, radix_bits=(6, 0), batch_launches=True), vjlib.options(passes=0, batch_launches=True))
+    for opts in variants:
         counts, out, p_off, status = run_batch(vjlib, ctx, cuda, rk, rp, sk, sp, r_off, s_off, caps, max_r=40_000, opts=opts)
         assert status == 0
         for j, (cnt, want) in enumerate(wants):
@@ -180,3 +186,65 @@ def test_batch_replays_in_a_cuda_graph(vjlib, ctx, cuda):
         want = vjlib.generate_join_expect(7000 + j, int(r_sizes[j]), int(s_sizes[j]), thr)
         assert int(counts[j].item()) == want[0]
         assert vjlib.pairs_digest(pairs[int(p_off[j]) :], want[0], 4) == (want[1], want[2]), j
+
+
+def test_batch_graph_holds_one_kernel_node(vjlib, ctx, cuda):
+    """A batch captured from a stream is one kernel node (the fused launch; the rest are
+    memsets and the status copy); replayed, every join equals the generator's expectation.
+    The separate-launch form of the same batch is many kernel nodes."""
+    import ctypes
+
+    import torch
+
+    try:
+        rt = ctypes.CDLL("libcudart.so.13")
+    except OSError:
+        pytest.skip("libcudart.so.13 not loadable")
+    rng = np.random.default_rng(37)
+    r_sizes = np.exp(rng.uniform(np.log(2.0**10), np.log(2.0**16), size=200)).astype(np.int64)
+    rk, rp, sk, sp, r_off, s_off, s_sizes, thr = _generated_batch(vjlib, cuda, 9000, r_sizes, 0.75)
+    p_off = np.concatenate([[0], np.cumsum(s_sizes)]).astype(np.uint64)
+    pairs = torch.zeros((int(p_off[-1]), 2), dtype=torch.int32, device=cuda)
+    counts = torch.zeros(r_sizes.size, dtype=torch.int64, device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    t_r = vjlib.table(rk, rp, rk.numel(), 1, 4)
+    t_s = vjlib.table(sk, sp, sk.numel(), 1, 4)
+    args = (t_r, t_s, int(r_sizes.size), dev(r_off, cuda), dev(s_off, cuda), pairs, dev(p_off, cuda), int(p_off[-1]), counts, status)
+    stream = torch.cuda.Stream()
+    h = ctypes.c_void_p(stream.cuda_stream)
+
+    def kernel_nodes(opts):
+        ctx.join_batch(*args, max_build_rows=int(r_sizes.max()), opts=opts, stream=stream)  # grows the workspace
+        torch.cuda.synchronize()
+        graph = ctypes.c_void_p()
+        assert rt.cudaStreamBeginCapture(h, 0) == 0
+        ctx.join_batch(*args, max_build_rows=int(r_sizes.max()), opts=opts, stream=stream)
+        assert rt.cudaStreamEndCapture(h, ctypes.byref(graph)) == 0
+        n = ctypes.c_size_t(0)
+        assert rt.cudaGraphGetNodes(graph, None, ctypes.byref(n)) == 0
+        nodes = (ctypes.c_void_p * n.value)()
+        assert rt.cudaGraphGetNodes(graph, nodes, ctypes.byref(n)) == 0
+        kinds = []
+        for nd in nodes:
+            t = ctypes.c_int(-1)
+            assert rt.cudaGraphNodeGetType(ctypes.c_void_p(nd), ctypes.byref(t)) == 0
+            kinds.append(t.value)
+        exe = ctypes.c_void_p()
+        assert rt.cudaGraphInstantiate(ctypes.byref(exe), graph, ctypes.c_ulonglong(0)) == 0
+        counts.zero_()
+        status.fill_(-1)
+        torch.cuda.synchronize()
+        for _ in range(2):
+            assert rt.cudaGraphLaunch(exe, h) == 0
+        assert rt.cudaStreamSynchronize(h) == 0
+        rt.cudaGraphExecDestroy(exe)
+        rt.cudaGraphDestroy(graph)
+        assert int(status.item()) == 0
+        for j in range(r_sizes.size):
+            want = vjlib.generate_join_expect(9000 + j, int(r_sizes[j]), int(s_sizes[j]), thr)
+            assert int(counts[j].item()) == want[0], j
+            assert vjlib.pairs_digest(pairs[int(p_off[j]) :], want[0], 4) == (want[1], want[2]), j
+        return kinds.count(0)  # cudaGraphNodeTypeKernel
+
+    assert kernel_nodes(None) == 1
+    assert kernel_nodes(vjlib.options(batch_launches=True)) >= 5

@@ -234,8 +234,9 @@ PassBufs carve_pass(Carver &c, int G, int bins, int max_units) {
 // One radix pass: histogram (per-unit counts, partition bounds, the next pass's plan) and
 // scatter (look-back cursors, bucket-sorted tiles). P's plan (device or host), sides,
 // segments, bucket rule and next_plan are the caller's; the bookkeeping comes from b.
-template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS>
-int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
+// The pass's bookkeeping in P; its counters, ticket and the segments' totals set to zero
+// (the histogram writes every unit's look-back words).
+int pass_setup(PassParams &P, const PassBufs &b, cudaStream_t stream) {
     const uint32_t bins = 1u << P.bits;
     P.ctl = b.ctl;
     P.seg_done = b.seg_done;
@@ -244,10 +245,15 @@ int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cu
     P.part_begin = b.part_begin;
     P.part_end = b.part_end;
     P.max_units = b.max_units;
-    profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
-    // counters, ticket and the segments' totals start at zero (the histogram writes every
-    // unit's look-back words)
     VJ_CUDA(cudaMemsetAsync(b.ctl, 0, (size_t)((char *)(b.seg_tot + (size_t)b.G * bins) - (char *)b.ctl), stream));
+    return VJ_OK;
+}
+
+template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS>
+int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cudaStream_t stream) {
+    const uint32_t bins = 1u << P.bits;
+    profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
+    VJ_TRY(pass_setup(P, b, stream));
     histogram_kernel<KW, PB, HS, IN_AOS><<<b.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_HIST_END + 4 * pass, stream);
@@ -343,6 +349,11 @@ struct JoinRun {
     uint32_t *batch_cnt = nullptr;
     uint32_t batch_parts = 1;
     bool plant_flag = false;  // VJ_JOIN_TEST_DEVICE_FLAG
+    // a batch as one fused launch (set before prepare): its parameters, grid and shared memory
+    bool fused = false;
+    BatchFusedParams fusedp{};
+    int fused_grid = 0;
+    size_t fused_smem = 0;
 };
 
 // VJ_JOIN_TEST_DEVICE_FLAG: sets a flag bit in the error word as a kernel that ran out of a
@@ -383,6 +394,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     uint16_t *bids[2] = {nullptr, nullptr};  // pass-2 buckets written by pass 1
     unsigned long long *b_out_begin = nullptr;
     uint32_t *item_join = nullptr;
+    uint32_t *gsync = nullptr;  // the fused batch's grid-barrier words, right after the error word
+    const bool fused = run->fused;
     auto layout = [&](Carver &c, void *bufs[2][2], PassBufs *pb0, PassBufs *pb1, uint32_t **item_begin, uint4 **item_desc, uint32_t **ticket, unsigned long long **out_count, uint32_t **error) {
         for (int pass = 0; pass < 2; pass++) {
             for (int sd = 0; sd < 2; sd++) {
@@ -405,6 +418,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         *ticket = c.take<uint32_t>(1);
         *out_count = c.take<unsigned long long>(1);
         *error = c.take<uint32_t>(1);
+        gsync = c.take<uint32_t>(2, 4);
     };
     void *bufs[2][2];
     PassBufs pb0{}, pb1{};
@@ -418,12 +432,16 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     Carver c;
     c.base = (char *)ws;
     layout(c, bufs, &pb0, &pb1, &item_begin, &item_desc, &ticket, &out_count, &error);
-    VJ_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), stream));
+    VJ_CUDA(cudaMemsetAsync(error, 0, fused ? 3 * sizeof(uint32_t) : sizeof(uint32_t), stream));
     ctx->launches = 0;
 
     const uint32_t *seg_begin = nullptr, *seg_end = nullptr;
     int Q = 1;
-    if (batch) {
+    if (batch && fused) {
+        seg_begin = b_seg_begin;
+        seg_end = b_seg_end;
+        Q = J;
+    } else if (batch) {
         batch_segments_kernel<<<(J + 256) / 256, 256, 0, stream>>>(in.joins, in.r_offsets, in.s_offsets, in.pair_offsets, in.rows[0], in.rows[1], in.pair_capacity, b_seg_begin, b_seg_end, b_out_begin,
                                                                      error);
         VJ_CUDA(cudaGetLastError());
@@ -465,7 +483,7 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
             host_plan(P, in.rows, 2);
         } else {
             P.plan = pb.plan;  // written by the previous pass, or by plan_kernel for a batch
-            if (pass == 0) {
+            if (pass == 0 && !fused) {
                 plan_kernel<<<1, PLAN_THREADS, 0, stream>>>(P, pb.plan);
                 VJ_CUDA(cudaGetLastError());
                 ctx->launches += 1;
@@ -475,7 +493,10 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
             P.next_plan = pb1.plan;
             P.next_max_units = pb1.max_units;
         }
-        if (pass == 0) {
+        if (fused) {
+            VJ_TRY(pass_setup(P, pb, stream));  // the fused launch runs the pass itself
+            run->fusedp.P = P;
+        } else if (pass == 0) {
             VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, ctx->info.sms, pass, P, pb, stream)));
         } else {
             VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, ctx->info.sms, pass, P, pb, stream)));
@@ -535,6 +556,29 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     run->plan_blocks = plan_blocks;
     run->d_out_count = out_count;
     run->d_error = error;
+    if (fused) {
+        BatchFusedParams &F = run->fusedp;
+        F.passes = (uint32_t)pl.passes;
+        F.joins = (uint32_t)J;
+        F.r_rows = in.rows[0];
+        F.s_rows = in.rows[1];
+        F.parts = (uint32_t)(np / J);
+        F.ro = in.r_offsets;
+        F.so = in.s_offsets;
+        F.po = in.pair_offsets;
+        F.pair_cap = in.pair_capacity;
+        F.seg_begin = b_seg_begin;
+        F.seg_end = b_seg_end;
+        F.out_begin = b_out_begin;
+        F.plan = pl.passes ? pb0.plan : nullptr;
+        F.cnt = b_cnt;
+        F.sync = gsync;
+        const size_t probe_smem = ProbeSmem<KW, PB, HS, true>::bytes(pl.rcap, pl.tcap, pl.scap);
+        run->fused_smem = batch_fused_smem<KW, PB, HS>(1u << pl.bits[0], probe_smem);
+        run->fused_grid = ctx->info.sms;
+        run->threads = PROBE_THREADS;
+        return VJ_OK;
+    }
     if (pl.passes == 0) {
         return batch ? probe_setup<KW, PB, HS, false, true>(ctx, pl, run) : probe_setup<KW, PB, HS, false, false>(ctx, pl, run);
     }
@@ -904,24 +948,39 @@ struct BuildProbeCall {
     }
 };
 
-// A batch of joins: one launch sequence, no host synchronisation. At most one radix pass
-// (the second pass's bookkeeping would grow with joins x buckets x buckets).
+// A batch of joins, no host synchronisation. At most one radix pass (the second pass's
+// bookkeeping would grow with joins x buckets x buckets). By default one fused,
+// cooperative launch runs it all (batch_fused_kernel); VJ_JOIN_BATCH_LAUNCHES runs the same
+// phases as separate launches.
 template <int KW, int PB, int HS>
-int batch_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, uint64_t max_build_rows, void *pairs, uint32_t *d_status, cudaStream_t stream) {
-    Plan pl = make_plan<KW, PB, HS>(max_build_rows, 4 * max_build_rows, ctx->info, opt);
+int batch_typed(vj_ctx *ctx, const Tables &t, const HashSpec &hs, const vj_join_options *opt, uint64_t max_build_rows, bool launches, void *pairs, uint32_t *d_status, cudaStream_t stream) {
+    const bool fused = HS == 0 && !launches;
+    DeviceInfo info = ctx->info;
+    if (fused && info.smem_optin > FUSED_SMEM + 1024) info.smem_optin = FUSED_SMEM + 1024;  // room for the phases' static shared memory
+    Plan pl = make_plan<KW, PB, HS>(max_build_rows, 4 * max_build_rows, info, opt);
     if (pl.passes == 2) {
         pl.passes = 1;
         pl.bits[0] = pl.bits[0] + pl.bits[1] > MAX_RADIX_BITS ? MAX_RADIX_BITS : pl.bits[0] + pl.bits[1];
         pl.bits[1] = 0;
     }
+    if (fused) pl.threads = PROBE_THREADS;  // the fused launch's blocks are PROBE_THREADS wide
     const bool prof = ctx->profiling;
     ctx->profiling = false;  // stage events need a synchronisation this call does not make
     JoinRun run;
+    run.fused = fused;
     int st = prepare<KW, PB, HS>(ctx, t, pl, hs, stream, &run);
     if (st == VJ_OK) {
         run.probe.out = pairs;
         run.probe.capacity = t.pair_capacity;
-        st = launch_probe<KW, PB, HS>(ctx, run, stream);
+        if (fused) {
+            if constexpr (HS == 0) {
+                run.fusedp.Q = run.probe;
+                st = batch_fused_launch<KW, PB, HS>(run.fusedp, run.fused_grid, run.fused_smem, stream);
+                ctx->launches = 1;
+            }
+        } else {
+            st = launch_probe<KW, PB, HS>(ctx, run, stream);
+        }
     }
     ctx->profiling = prof;
     VJ_TRY(st);
@@ -946,12 +1005,13 @@ struct BatchCall {
     HashSpec hs;
     const vj_join_options *opt;
     uint64_t max_build_rows;
+    bool launches;  // VJ_JOIN_BATCH_LAUNCHES: separate launches instead of the fused one
     void *pairs;
     uint32_t *status;
     cudaStream_t stream;
     template <int KW, int PB, int HS>
     int run() {
-        return batch_typed<KW, PB, HS>(ctx, t, hs, opt, max_build_rows, pairs, status, stream);
+        return batch_typed<KW, PB, HS>(ctx, t, hs, opt, max_build_rows, launches, pairs, status, stream);
     }
 };
 
@@ -1029,6 +1089,7 @@ extern "C" int vj_join_batch(vj_ctx *ctx, const vj_table *r, const vj_table *s, 
     rmax.rows = call.max_build_rows;
     smax.rows = (uint64_t)((double)call.max_build_rows * ((double)s->rows / (double)r->rows)) + 1;
     call.opt = tuned_options(ctx, &rmax, &smax, options);
+    call.launches = options && (options->flags & VJ_JOIN_BATCH_LAUNCHES);
     call.pairs = d_pairs;
     call.status = d_status;
     call.stream = st;

@@ -423,7 +423,7 @@ __device__ __forceinline__ UnitRange unit_range(const PassParams &P, uint32_t u)
 // segment, so that every segment's bounds are written by its last unit. plan[0] = target,
 // plan[1 + g] = the first unit of g, plan[1 + G] = all units. target is the larger of
 // min_rows and the rows that spread the segments over max_units - G units.
-__device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t G, uint32_t max_units, uint32_t min_rows, uint32_t *plan) {
+static __device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t G, uint32_t max_units, uint32_t min_rows, uint32_t *plan) {
     __shared__ unsigned long long s_w64[32];
     __shared__ uint32_t s_w32[32];
     __shared__ uint32_t s_target;
@@ -462,7 +462,7 @@ __device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t 
 }
 
 // One block: the unit plan of a pass over device segments (batches of joins).
-__global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(PassParams P, uint32_t *plan) {
+static __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(PassParams P, uint32_t *plan) {
     plan_block(P.seg_begin, P.seg_end, (uint32_t)(P.nsides * P.Q), (uint32_t)P.max_units, P.min_unit_rows, plan);
 }
 
@@ -501,22 +501,27 @@ __device__ __forceinline__ uint64_t global_row_hash(const Side &S, uint32_t i, c
     return row_hash<KW>(load_key_stream<KW>(S.keys_in, i), hs);
 }
 
-// Grid: one block per unit of the plan (blocks past the plan's units leave at once). Four
-// blocks per SM (32 registers a thread) keep enough loads in flight.
-template <int KW, int PB, int HS, bool AOS>
-__global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P) {
-    extern __shared__ uint32_t s_hist[];
-    __shared__ uint32_t s_last;
-    __shared__ uint32_t s_warp[32];
-    __shared__ UnitRange s_unit;  // kept in shared memory: no registers held across the count
+// Block scratch of the histogram: the unit (kept in shared memory, so no registers are held
+// across the count), the block-scan words and the last-unit flag.
+struct HistShared {
+    UnitRange unit;
+    uint32_t u;
+    uint32_t warp[32];
+    uint32_t last;
+};
+
+// Counts of unit u by the whole block (NT threads); s_hist holds 2^bits words.
+template <int KW, int PB, int HS, bool AOS, int NT>
+__device__ __forceinline__ void histogram_unit(const PassParams &P, uint32_t u, uint32_t *s_hist, HistShared &sh) {
     const uint32_t bins = 1u << P.bits;
     const uint64_t mask = bins - 1;
-    const uint32_t u = blockIdx.x;
-    if (u >= plan_total(P)) return;
-    if (threadIdx.x == 0) s_unit = unit_range(P, u);
-    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) s_hist[b] = 0;
+    if (threadIdx.x == 0) {
+        sh.unit = unit_range(P, u);
+        sh.u = u;
+    }
+    for (uint32_t b = threadIdx.x; b < bins; b += NT) s_hist[b] = 0;
     __syncthreads();
-    const UnitRange &U = s_unit;
+    const UnitRange &U = sh.unit;
     const Side &S = P.side[U.side];
 
     // ---- count
@@ -524,33 +529,33 @@ __global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P
         // buckets written by the previous pass: 2 bytes a row instead of the row
         constexpr int UB = 8;
         uint32_t i = U.a + threadIdx.x;
-        for (; i + (UB - 1) * PART_THREADS < U.b; i += UB * PART_THREADS) {
+        for (; i + (UB - 1) * NT < U.b; i += UB * NT) {
             uint32_t v[UB];
 #pragma unroll
-            for (int k = 0; k < UB; k++) v[k] = __ldcs(S.bid_in + i + k * PART_THREADS);
+            for (int k = 0; k < UB; k++) v[k] = __ldcs(S.bid_in + i + k * NT);
 #pragma unroll
             for (int k = 0; k < UB; k++) atomicAdd(&s_hist[v[k] & mask], 1u);
         }
-        for (; i < U.b; i += PART_THREADS) atomicAdd(&s_hist[__ldcs(S.bid_in + i) & mask], 1u);
+        for (; i < U.b; i += NT) atomicAdd(&s_hist[__ldcs(S.bid_in + i) & mask], 1u);
     } else {
         constexpr int UNROLL = 4;
-        constexpr uint32_t STEP = UNROLL * PART_THREADS;
+        constexpr uint32_t STEP = UNROLL * NT;
         // keep the next AHEAD steps of this unit on their way to L2
         constexpr uint32_t AHEAD = 4;
         if (threadIdx.x == 0) histogram_prefetch<KW, PB, HS, AOS>(S, U.a, min(U.b, U.a + AHEAD * STEP));
         uint32_t i = U.a + threadIdx.x;
-        for (; i + (UNROLL - 1) * PART_THREADS < U.b; i += UNROLL * PART_THREADS) {
+        for (; i + (UNROLL - 1) * NT < U.b; i += UNROLL * NT) {
             if (threadIdx.x == 0) {
                 const uint32_t pa = i + AHEAD * STEP;
                 if (pa < U.b) histogram_prefetch<KW, PB, HS, AOS>(S, pa, min(U.b, pa + STEP));
             }
             uint64_t h[UNROLL];
 #pragma unroll
-            for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * PART_THREADS, P.hs);
+            for (int k = 0; k < UNROLL; k++) h[k] = global_row_hash<KW, PB, HS, AOS>(S, i + k * NT, P.hs);
 #pragma unroll
             for (int k = 0; k < UNROLL; k++) atomicAdd(&s_hist[(bucket_hash(h[k], P.hs) >> P.shift) & mask], 1u);
         }
-        for (; i < U.b; i += PART_THREADS) {
+        for (; i < U.b; i += NT) {
             atomicAdd(&s_hist[(bucket_hash(global_row_hash<KW, PB, HS, AOS>(S, i, P.hs), P.hs) >> P.shift) & mask], 1u);
         }
     }
@@ -558,8 +563,8 @@ __global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P
 
     // ---- publish: the unit's counts (its look-back words; the segment's first unit's are
     // already its inclusive prefix) and the segment's totals
-    unsigned long long *L = P.look + (size_t)u * bins;
-    for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
+    unsigned long long *L = P.look + (size_t)sh.u * bins;
+    for (uint32_t b = threadIdx.x; b < bins; b += NT) {
         const uint32_t c = s_hist[b];
         L[b] = lb_pack(U.first ? LB_INC : LB_AGG, c);
         if (c) atomicAdd(&P.seg_tot[(size_t)U.g * bins + b], c);
@@ -569,18 +574,18 @@ __global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        s_last = atomicAdd(&P.seg_done[U.g], 1u) + 1 == seg_units(P, U.g);
+        sh.last = atomicAdd(&P.seg_done[U.g], 1u) + 1 == seg_units(P, U.g);
     }
     __syncthreads();
     // ---- the segment's last unit counted: partition bounds of the segment
-    if (s_last) {
+    if (sh.last) {
         __threadfence();
         const uint32_t *tot = P.seg_tot + (size_t)U.g * bins;
-        const uint32_t per = (bins + PART_THREADS - 1) / PART_THREADS;
+        const uint32_t per = (bins + NT - 1) / NT;
         const uint32_t b0 = threadIdx.x * per;
         uint32_t mine = 0;
         for (uint32_t b = b0; b < b0 + per && b < bins; b++) mine += __ldcg(tot + b);
-        uint32_t run = block_exclusive_scan<uint32_t>(mine, s_warp, nullptr);
+        uint32_t run = block_exclusive_scan<uint32_t>(mine, sh.warp, nullptr);
         run += P.seg_begin ? P.seg_begin[U.g] : 0;
         for (uint32_t b = b0; b < b0 + per && b < bins; b++) {
             P.part_begin[(size_t)U.g * bins + b] = run;
@@ -594,27 +599,37 @@ __global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
-            s_last = atomicAdd(&P.ctl[0], 1u) + 1 == plan_total(P);
+            sh.last = atomicAdd(&P.ctl[0], 1u) + 1 == plan_total(P);
         }
         __syncthreads();
-        if (s_last) {
+        if (sh.last) {
             __threadfence();
             plan_block(P.part_begin, P.part_end, (uint32_t)(P.nsides * P.Q) * bins, (uint32_t)P.next_max_units, P.min_unit_rows, P.next_plan);
         }
     }
 }
 
+// Grid: one block per unit of the plan (blocks past the plan's units leave at once). Four
+// blocks per SM (32 registers a thread) keep enough loads in flight.
+template <int KW, int PB, int HS, bool AOS>
+__global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P) {
+    extern __shared__ uint32_t s_hist[];
+    __shared__ HistShared sh;
+    if (blockIdx.x >= plan_total(P)) return;
+    histogram_unit<KW, PB, HS, AOS, PART_THREADS>(P, blockIdx.x, s_hist, sh);
+}
+
 // Shared memory of the scatter kernel: two input tiles filled by bulk copies, the
 // bucket-sorted output tile (row-contiguous), each sorted row's bucket, and per bucket the
 // tile's counts (two tiles), its start in the sorted tile and the unit's write cursor.
-template <int KW, int PB, int HS, bool IN_AOS, int ITEMS>
+template <int KW, int PB, int HS, bool IN_AOS, int ITEMS, int NT = PART_THREADS>
 struct ScatterSmem {
     using L = Layout<KW, PB, HS>;
-    static constexpr int T = PART_THREADS * ITEMS;
+    static constexpr int T = NT * ITEMS;
     static constexpr size_t IN_BUF = Chunk<KW, PB, HS, IN_AOS>::bytes(T);
     static constexpr size_t OUT = (size_t)T * (L::STRIDE + 4);  // rows + bucket word per row
     // + per bucket: counts of two tiles, start, cursor; chunk totals past 1024 buckets
-    static size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 4 * 4 + (bins > 1024 ? bins / 32 * 4 : 0); }
+    static constexpr size_t bytes(uint32_t bins) { return 16 + 2 * IN_BUF + OUT + (size_t)bins * 4 * 4 + (bins > 1024 ? bins / 32 * 4 : 0); }
 };
 
 // Rows per thread of a scatter tile: the largest of 4, 2, 1 whose block (with 2^9 bins)
@@ -713,14 +728,21 @@ __device__ __forceinline__ void scatter_issue(const PassParams &P, TileIssuer &i
     is.fresh = false;
 }
 
-template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS>
-__global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
+// Block scratch of the scatter: the two tiles' descriptors and window offsets.
+struct ScatterShared {
+    TileDesc tile[2];
+    uint32_t delta[2][3];
+};
+
+// The scatter of a pass by the whole block (NT threads) until the units run out; s_raw is
+// the block's ScatterSmem<..., NT>::bytes(bins) of dynamic shared memory (128-byte aligned).
+template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS, int NT>
+__device__ __forceinline__ void scatter_run(const PassParams &P, unsigned char *s_raw, ScatterShared &sh) {
     using L = Layout<KW, PB, HS>;
     using C = Chunk<KW, PB, HS, IN_AOS>;
     using Pt = typename PayloadType<PB>::T;
-    using SM = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS>;
+    using SM = ScatterSmem<KW, PB, HS, IN_AOS, ITEMS, NT>;
     constexpr int T = SM::T;
-    extern __shared__ __align__(128) unsigned char s_raw[];
     uint64_t *bar = (uint64_t *)s_raw;
     unsigned char *inb0 = s_raw + 16;
     unsigned char *out_rows = inb0 + 2 * SM::IN_BUF;
@@ -731,13 +753,13 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     uint32_t *s_start = s_cnt + 2 * bins;  // [bins]: bucket start in the sorted tile
     uint32_t *s_run = s_start + bins;      // [bins]: output row of the tile's first row of the bucket
     uint32_t *s_chunk = s_run + bins;      // [bins / 32]: chunk totals (more than 1024 buckets)
-    __shared__ TileDesc s_tile[2];
-    __shared__ uint32_t s_delta[2][3];
+    TileDesc *s_tile = sh.tile;
+    uint32_t (*s_delta)[3] = sh.delta;
     const uint32_t total = plan_total(P);
     const uint64_t mask = bins - 1;
     const uint64_t nmask = (1ull << P.next_bits) - 1;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr uint32_t NW = PART_THREADS / 32;
+    constexpr uint32_t NW = NT / 32;
 
     TileIssuer is;
     if (threadIdx.x == 0) {
@@ -745,7 +767,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         mbar_init(&bar[1], 1);
         fence_proxy_async();
     }
-    for (uint32_t b = threadIdx.x; b < 2 * bins; b += PART_THREADS) s_cnt[b] = 0;
+    for (uint32_t b = threadIdx.x; b < 2 * bins; b += NT) s_cnt[b] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
         scatter_issue<KW, PB, HS, IN_AOS, T>(P, is, total, inb0, &bar[0], &s_tile[0], s_delta[0]);
@@ -771,7 +793,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         if (ok && !end) {
 #pragma unroll
             for (int j = 0; j < ITEMS; j++) {
-                const uint32_t i = j * PART_THREADS + threadIdx.x;
+                const uint32_t i = j * NT + threadIdx.x;
                 if (i < nt) {
                     const uint64_t mh = bucket_hash(in.h_of(i, P.hs), P.hs);
                     const uint32_t b = (uint32_t)((mh >> P.shift) & mask);
@@ -794,7 +816,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         // previous tile's counts added), the previous tile's counts cleared, the start of the
         // bucket's rows in the sorted tile
         const uint32_t g = D.gs & 0x3fffffffu;
-        for (uint32_t b = threadIdx.x; b < bins; b += PART_THREADS) {
+        for (uint32_t b = threadIdx.x; b < bins; b += NT) {
             if (fresh) s_run[b] = P.part_begin[(size_t)g * bins + b] + (b == threadIdx.x ? lb0 : (uint32_t)look_back_far(P, D.unit, D.rank, b, bins));
             else s_run[b] += cnt_prev[b];
             cnt_prev[b] = 0;
@@ -846,7 +868,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         // ---- rows into bucket order
 #pragma unroll
         for (int j = 0; j < ITEMS; j++) {
-            const uint32_t i = j * PART_THREADS + threadIdx.x;
+            const uint32_t i = j * NT + threadIdx.x;
             if (i < nt) {
                 const uint32_t pos = s_start[bk[j] & 0xffffu] + rk[j];
                 in.copy_row(i, out_rows + (size_t)pos * L::STRIDE);
@@ -856,7 +878,7 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
         __syncthreads();  // input buffer `buf` is free: refill it
         if (threadIdx.x == 0) scatter_issue<KW, PB, HS, IN_AOS, T>(P, is, total, inb0 + buf * SM::IN_BUF, &bar[buf], &s_tile[buf], s_delta[buf]);
         // ---- bucket runs out: row i of the sorted tile goes to cursor + (i - bucket start)
-        for (uint32_t i = threadIdx.x; i < nt; i += PART_THREADS) {
+        for (uint32_t i = threadIdx.x; i < nt; i += NT) {
             const uint32_t sbk = st_b[i];
             const uint32_t b = sbk & 0xffffu;
             const uint32_t dst = s_run[b] + i - s_start[b];
@@ -883,6 +905,13 @@ __global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
     }
 }
 
+template <int KW, int PB, int HS, bool IN_AOS, bool OUT_AOS, int ITEMS>
+__global__ void __launch_bounds__(PART_THREADS) scatter_kernel(PassParams P) {
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    __shared__ ScatterShared sh;
+    scatter_run<KW, PB, HS, IN_AOS, OUT_AOS, ITEMS, PART_THREADS>(P, s_raw, sh);
+}
+
 // ------------------------------------------------------------------ probe kernels
 
 // Work items of partition p: (build chunks) x (probe chunks), 0 if either side is empty.
@@ -900,7 +929,7 @@ __device__ __forceinline__ unsigned long long items_of(const ProbeParams &Q, int
 // no items.
 constexpr int PLAN_BLOCK = 256;
 
-__global__ void __launch_bounds__(PLAN_BLOCK) items_count_kernel(ProbeParams Q, unsigned long long *block_tot) {
+static __global__ void __launch_bounds__(PLAN_BLOCK) items_count_kernel(ProbeParams Q, unsigned long long *block_tot) {
     __shared__ unsigned long long s_warp[32];
     const int p = blockIdx.x * PLAN_BLOCK + threadIdx.x;
     const unsigned long long n = p < Q.np ? items_of(Q, p) : 0ull;
@@ -910,7 +939,7 @@ __global__ void __launch_bounds__(PLAN_BLOCK) items_count_kernel(ProbeParams Q, 
     if (threadIdx.x == 0) block_tot[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(PLAN_THREADS) items_scan_kernel(ProbeParams Q, unsigned long long *block_tot, int nblocks) {
+static __global__ void __launch_bounds__(PLAN_THREADS) items_scan_kernel(ProbeParams Q, unsigned long long *block_tot, int nblocks) {
     __shared__ unsigned long long s_warp[32];
     const int per = (nblocks + PLAN_THREADS - 1) / PLAN_THREADS;
     const int b0 = threadIdx.x * per;
@@ -934,7 +963,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) items_scan_kernel(ProbeParams Q,
     }
 }
 
-__global__ void __launch_bounds__(PLAN_BLOCK) items_write_kernel(ProbeParams Q, const unsigned long long *block_base) {
+static __global__ void __launch_bounds__(PLAN_BLOCK) items_write_kernel(ProbeParams Q, const unsigned long long *block_base) {
     const int p = blockIdx.x * PLAN_BLOCK + threadIdx.x;
     if (p >= Q.np) return;
     unsigned long long run = block_base[blockIdx.x] + Q.item_begin[p];
@@ -994,12 +1023,10 @@ __device__ __forceinline__ uint32_t batch_group_items(const ProbeParams &Q, cons
     return ((d.y - d.x + Q.rcap - 1) / Q.rcap) * ((d.w - d.z + Q.schunk - 1) / Q.schunk);
 }
 
-// Grid: one block per join. COUNT: items of join j -> cnt[j]. !COUNT: its item
-// descriptors from base[j] on (none past item_cap).
+// Join j by the whole block. COUNT: its items -> cnt[j]. !COUNT: its item descriptors from
+// base[j] on (none past item_cap). s_warp: 32 words of block scratch.
 template <bool COUNT>
-__global__ void __launch_bounds__(256) batch_items_kernel(ProbeParams Q, uint32_t parts, uint32_t *cnt, const uint32_t *base) {
-    __shared__ uint32_t s_warp[32];
-    const uint32_t j = blockIdx.x;
+__device__ __forceinline__ void batch_items_join(const ProbeParams &Q, uint32_t parts, uint32_t *cnt, const uint32_t *base, uint32_t j, uint32_t *s_warp) {
     const BatchGroups bg = batch_groups(Q, parts, j);
     uint32_t run = COUNT ? 0u : base[j];
     for (uint32_t g0 = 0; g0 < bg.groups; g0 += blockDim.x) {
@@ -1030,9 +1057,16 @@ __global__ void __launch_bounds__(256) batch_items_kernel(ProbeParams Q, uint32_
     if (COUNT && threadIdx.x == 0) cnt[j] = run;
 }
 
-// One block: item offset of every join, the item total, the counters reset. A batch with
-// more items than item_desc holds is refused (error flag 2, no items).
-__global__ void __launch_bounds__(PLAN_THREADS) batch_scan_kernel(ProbeParams Q, uint32_t *cnt_base) {
+// Grid: one block per join.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) batch_items_kernel(ProbeParams Q, uint32_t parts, uint32_t *cnt, const uint32_t *base) {
+    __shared__ uint32_t s_warp[32];
+    batch_items_join<COUNT>(Q, parts, cnt, base, blockIdx.x, s_warp);
+}
+
+// One block of PLAN_THREADS: item offset of every join, the item total, the counters reset.
+// A batch with more items than item_desc holds is refused (error flag 2, no items).
+__device__ __forceinline__ void batch_scan_block(const ProbeParams &Q, uint32_t *cnt_base) {
     __shared__ unsigned long long s_warp[32];
     const uint32_t per = (Q.joins + PLAN_THREADS - 1) / PLAN_THREADS;
     const uint32_t j0 = threadIdx.x * per;
@@ -1055,6 +1089,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) batch_scan_kernel(ProbeParams Q,
         *Q.out_count = 0;
     }
 }
+
+static __global__ void __launch_bounds__(PLAN_THREADS) batch_scan_kernel(ProbeParams Q, uint32_t *cnt_base) { batch_scan_block(Q, cnt_base); }
 
 template <int PB>
 struct Pair;
@@ -1235,16 +1271,17 @@ __device__ __forceinline__ void flush_stage(const ProbeParams &Q, const typename
     __syncwarp();
 }
 
-// BATCH: a batch of joins; each item's pairs go to its join's output range.
+// The probe by the whole block (blockDim.x threads, the last warp the producer) until the
+// items run out; s_raw is the block's ProbeSmem bytes of dynamic shared memory. BATCH: a
+// batch of joins; each item's pairs go to its join's output range.
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
-__global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) {
+__device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s_raw) {
     using C = Chunk<KW, PB, HS, AOS>;
     using Pt = typename PayloadType<PB>::T;
     using PT = typename Pair<PB>::T;
     using SM = ProbeSmem<KW, PB, HS, AOS>;
     using Row = ProbeRow<KW, PB, HS>;
     constexpr int J = PROBE_J;
-    extern __shared__ __align__(128) unsigned char s_raw[];
     uint64_t *full = (uint64_t *)s_raw;  // [2]: build rows landed + descriptor published
     uint64_t *empty = full + 2;          // [2]: consumers done with the item
     const size_t rbytes = SM::rbuf_bytes(Q.rcap);
@@ -1379,9 +1416,12 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
         const uint32_t cmask = cap - 1;
         const C R = C::view(rbuf0 + b * rbytes, Q.rcap, s_rdelta[b]);
         // ---- build: slot = tag << 11 | row; an equal key met on the way marks the item as
-        // having duplicate build keys
+        // having duplicate build keys. Build rows go to the consumers in reverse order: the
+        // rows past the first NC land on the last warps, while the probe rows past a whole
+        // number of rounds land on the first ones, so no warp carries both extras to the
+        // table barrier (4.81 -> 4.54 ms for the 2^27 x 2^29 join's probe).
         bool dup = false;
-        for (uint32_t i = c; i < nr; i += NC) {
+        for (uint32_t i = NC - 1 - c; i < nr; i += NC) {
             const Key<KW> key = R.key(i);
             const uint64_t h = HS ? R.hash(i) : row_hash<KW>(key, Q.hs);
             uint32_t slot = (uint32_t)(mix_hash(h) >> Q.slot_shift) & cmask;
@@ -1508,6 +1548,198 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) 
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[b]);
     }
+}
+
+template <int KW, int PB, int HS, bool AOS, bool BATCH>
+__global__ void __launch_bounds__(PROBE_THREADS, 1) probe_kernel(ProbeParams Q) {
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    probe_run<KW, PB, HS, AOS, BATCH>(Q, s_raw);
+}
+
+
+// ------------------------------------------------------------------ fused batch of joins
+//
+// A batch of joins as one persistent launch (cooperative: every block resident, one per
+// SM, PROBE_THREADS threads): the phases of the separate launches run back to back inside
+// the kernel, each over the whole grid, with a grid barrier between them --
+//   segments      every join's row ranges, clamped into the tables (flag 16 if clamped)
+//   plan          block 0: the output ranges made non-decreasing; the pass's unit plan
+//   histogram     (one radix pass) the units' counts, the partition bounds
+//   scatter       (one radix pass) rows into partitions, 4096-row tiles
+//   items         per join: items counted; block 0: their offsets; per join: descriptors
+//   probe         build and probe, pairs into each join's output range
+// A block whose barrier wait runs out (WAIT_NS) sets error flag 64 and leaves; the others'
+// waits then run out too, so the launch always ends.
+
+// Row ranges of join j of a batch from the caller's offsets, each clamped into its table
+// (and the output range into the output buffer) so that no later phase can leave its
+// buffers; error flag 16 when an offset had to be clamped. j in [0, joins].
+__device__ __forceinline__ void batch_segment(uint32_t j, uint32_t joins, const unsigned long long *ro, const unsigned long long *so, const unsigned long long *po, uint32_t r_rows,
+                                              uint32_t s_rows, unsigned long long pair_cap, uint32_t *seg_begin, uint32_t *seg_end, unsigned long long *out_begin, uint32_t *error) {
+    bool bad = false;
+    auto clamp = [&](unsigned long long v, unsigned long long lo, unsigned long long hi) -> unsigned long long {
+        const unsigned long long c = v < lo ? lo : (v > hi ? hi : v);
+        bad |= c != v;
+        return c;
+    };
+    // ranges start at 0, end at the table's rows and never decrease
+    out_begin[j] = clamp(po[j], 0, pair_cap);
+    if (j < joins) {
+        const unsigned long long rb = j == 0 ? clamp(ro[0], 0, 0) : clamp(ro[j], 0, r_rows);
+        const unsigned long long sb = j == 0 ? clamp(so[0], 0, 0) : clamp(so[j], 0, s_rows);
+        const unsigned long long re = j + 1 == joins ? clamp(ro[j + 1], r_rows, r_rows) : clamp(ro[j + 1], rb, r_rows);
+        const unsigned long long se = j + 1 == joins ? clamp(so[j + 1], s_rows, s_rows) : clamp(so[j + 1], sb, s_rows);
+        bad |= po[j + 1] < po[j];
+        seg_begin[j] = (uint32_t)rb;
+        seg_end[j] = (uint32_t)(re < rb ? rb : re);
+        seg_begin[joins + j] = (uint32_t)sb;
+        seg_end[joins + j] = (uint32_t)(se < sb ? sb : se);
+    }
+    if (bad) atomicOr(error, 16u);
+}
+
+// Whole block: out_begin[0..joins] made non-decreasing (a running maximum).
+__device__ __forceinline__ void out_monotone_block(uint32_t joins, unsigned long long *out_begin) {
+    __shared__ unsigned long long s_max[32];
+    const uint32_t n = joins + 1, per = (n + blockDim.x - 1) / blockDim.x, a = threadIdx.x * per;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    unsigned long long m = 0;
+    for (uint32_t i = a; i < a + per && i < n; i++) m = max(m, out_begin[i]);
+    // exclusive maximum over the threads before this one
+    unsigned long long x = m;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((int)lane >= o) x = max(x, y);
+    }
+    if (lane == 31) s_max[warp] = x;
+    __syncthreads();
+    unsigned long long run = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) run = 0;
+    for (uint32_t w = 0; w < warp && w < nwarps; w++) run = max(run, s_max[w]);
+    for (uint32_t i = a; i < a + per && i < n; i++) {
+        run = max(run, out_begin[i]);
+        out_begin[i] = run;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) { asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory"); }
+
+// Grid barrier of a cooperative launch: words[0] counts arrivals (zero at launch, back to
+// zero after every barrier), words[1] is the generation. False (error flag 64 set) when
+// the wait ran out.
+__device__ __forceinline__ bool grid_sync(uint32_t *words, uint32_t *error) {
+    __shared__ uint32_t s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool ok = true;
+        const uint32_t gen = ld_acquire_u32(words + 1);
+        __threadfence();  // this block's writes before its arrival
+        if (atomicAdd(words, 1u) + 1u == gridDim.x) {
+            words[0] = 0;
+            __threadfence();
+            st_release_u32(words + 1, gen + 1u);
+        } else {
+            const uint64_t t0 = global_ns();
+            while (ld_acquire_u32(words + 1) == gen) {
+                if (global_ns() - t0 > WAIT_NS) {
+                    atomicOr(error, 64u);
+                    ok = false;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct BatchFusedParams {
+    PassParams P;   // the radix pass (passes == 1)
+    ProbeParams Q;  // the probe; Q.error is the batch's error word
+    uint32_t passes, joins, r_rows, s_rows, parts;
+    const unsigned long long *ro, *so, *po;
+    unsigned long long pair_cap;
+    uint32_t *seg_begin, *seg_end;  // [2 * joins]: join rows per side
+    unsigned long long *out_begin;  // [joins + 1]
+    uint32_t *plan;                 // the pass's unit plan
+    uint32_t *cnt;                  // [joins]: items per join, then their offsets
+    uint32_t *sync;                 // grid barrier words (zero at launch)
+};
+
+// Dynamic shared memory the fused launch may take: the 227 KB a block may opt into, less
+// room for the phases' static shared memory.
+constexpr size_t FUSED_SMEM = 227 * 1024 - 4096;
+
+// Rows per thread of the fused launch's scatter tiles: the largest of 4, 2, 1 whose tile
+// fits FUSED_SMEM with the widest pass (2^MAX_RADIX_BITS buckets).
+template <int KW, int PB, int HS>
+constexpr int fused_scatter_items() {
+    return ScatterSmem<KW, PB, HS, false, 4, PROBE_THREADS>::bytes(1u << MAX_RADIX_BITS) <= FUSED_SMEM   ? 4
+           : ScatterSmem<KW, PB, HS, false, 2, PROBE_THREADS>::bytes(1u << MAX_RADIX_BITS) <= FUSED_SMEM ? 2
+                                                                                                        : 1;
+}
+
+template <int KW, int PB, int HS, bool AOS>
+__global__ void __launch_bounds__(PROBE_THREADS, 1) batch_fused_kernel(BatchFusedParams F) {
+    static_assert(PLAN_THREADS == PROBE_THREADS, "the fused launch's blocks run the block-wide planners");
+    constexpr int ITEMS = fused_scatter_items<KW, PB, HS>();
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    __shared__ HistShared hsh;
+    __shared__ ScatterShared ssh;
+    __shared__ uint32_t s_w32[32];
+    uint32_t *error = F.Q.error;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j <= F.joins; j += nthreads)
+        batch_segment(j, F.joins, F.ro, F.so, F.po, F.r_rows, F.s_rows, F.pair_cap, F.seg_begin, F.seg_end, F.out_begin, error);
+    if (!grid_sync(F.sync, error)) return;
+    if (blockIdx.x == 0) {
+        out_monotone_block(F.joins, F.out_begin);
+        if (AOS) plan_block(F.seg_begin, F.seg_end, 2 * F.joins, (uint32_t)F.P.max_units, F.P.min_unit_rows, F.plan);
+    }
+    if (!grid_sync(F.sync, error)) return;
+    if (AOS) {
+        const uint32_t units = plan_total(F.P);
+        for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
+            histogram_unit<KW, PB, HS, false, PROBE_THREADS>(F.P, u, (uint32_t *)s_raw, hsh);
+            __syncthreads();
+        }
+        if (!grid_sync(F.sync, error)) return;
+        fence_proxy_async();  // the histogram's shared memory is refilled by bulk copies next
+        scatter_run<KW, PB, HS, false, true, ITEMS, PROBE_THREADS>(F.P, s_raw, ssh);
+        if (!grid_sync(F.sync, error)) return;
+    }
+    for (uint32_t j = blockIdx.x; j < F.joins; j += gridDim.x) batch_items_join<true>(F.Q, F.parts, F.cnt, nullptr, j, s_w32);
+    if (!grid_sync(F.sync, error)) return;
+    if (blockIdx.x == 0) batch_scan_block(F.Q, F.cnt);
+    if (!grid_sync(F.sync, error)) return;
+    for (uint32_t j = blockIdx.x; j < F.joins; j += gridDim.x) batch_items_join<false>(F.Q, F.parts, nullptr, F.cnt, j, s_w32);
+    if (!grid_sync(F.sync, error)) return;
+    fence_proxy_async();  // likewise the scatter's, before the probe's bulk copies
+    __syncthreads();
+    probe_run<KW, PB, HS, AOS, true>(F.Q, s_raw);
+}
+
+// Host launch of the fused batch (csrc/vj_batch.cu): cooperative, `grid` blocks of
+// PROBE_THREADS with `smem` bytes of dynamic shared memory.
+template <int KW, int PB, int HS>
+int batch_fused_launch(const BatchFusedParams &F, int grid, size_t smem, cudaStream_t stream);
+
+// Dynamic shared memory of the fused batch: the largest phase's.
+template <int KW, int PB, int HS>
+size_t batch_fused_smem(uint32_t bins, size_t probe_smem) {
+    const size_t sc = ScatterSmem<KW, PB, HS, false, fused_scatter_items<KW, PB, HS>(), PROBE_THREADS>::bytes(bins);
+    size_t m = probe_smem > sc ? probe_smem : sc;
+    return m > (size_t)bins * 4 ? m : (size_t)bins * 4;
 }
 
 }  // namespace vj

@@ -28,7 +28,7 @@ int lg(uint64_t x) {
 
 bool automatic(const vj_join_options *o) {
     if (!o) return true;
-    return o->flags == 0 && o->passes == 0 && o->radix_bits[0] == 0 && o->radix_bits[1] == 0 && o->build_rows == 0 && o->probe_rows == 0 && o->probe_threads == 0 && o->probe_sub_rows == 0 &&
+    return (o->flags & ~VJ_JOIN_BATCH_LAUNCHES) == 0 && o->passes == 0 && o->radix_bits[0] == 0 && o->radix_bits[1] == 0 && o->build_rows == 0 && o->probe_rows == 0 && o->probe_threads == 0 && o->probe_sub_rows == 0 &&
            o->table_load_pct == 0;
 }
 

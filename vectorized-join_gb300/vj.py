@@ -24,6 +24,7 @@ VJ_JOIN_FIXED_PASSES = 1
 VJ_JOIN_SHARED_TABLES = 2
 VJ_JOIN_L2_TABLES = 4
 VJ_JOIN_TEST_DEVICE_FLAG = 1 << 16
+VJ_JOIN_BATCH_LAUNCHES = 1 << 17
 
 ALGORITHMS = [
     "fnv",
@@ -342,15 +343,18 @@ def table(keys, payloads, rows: int, key_words: int, payload_bytes: int) -> VjTa
     return t
 
 
-def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, table_load_pct: int = 0, tables: str = "auto", test_device_flag: bool = False) -> VjJoinOptions:
+def options(hash_algo: int = 0, hash_bits: int = 0, passes: int | None = None, radix_bits=(0, 0), build_rows: int = 0, probe_rows: int = 0, probe_threads: int = 0, table_load_pct: int = 0, tables: str = "auto", test_device_flag: bool = False, batch_launches: bool = False) -> VjJoinOptions:
     """Join options; tables: "auto" or "shared" (shared-memory tables; "l2" is refused by the
-    library with VJ_ERR_UNSUPPORTED)."""
+    library with VJ_ERR_UNSUPPORTED). batch_launches: vj_join_batch as separate launches
+    instead of one fused launch."""
     o = VjJoinOptions()
     o.hash_algo = hash_algo
     o.hash_bits = hash_bits
     o.flags = {"auto": 0, "shared": VJ_JOIN_SHARED_TABLES, "l2": VJ_JOIN_L2_TABLES}[tables]
     if test_device_flag:
         o.flags |= VJ_JOIN_TEST_DEVICE_FLAG
+    if batch_launches:
+        o.flags |= VJ_JOIN_BATCH_LAUNCHES
     if passes is not None:
         o.flags |= VJ_JOIN_FIXED_PASSES
         o.passes = passes
