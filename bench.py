@@ -447,9 +447,9 @@ def run_batch_join(args) -> None:
     vj = _import(PKG / "vj.py", "vj")
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    joins = 4096
+    joins = 4096 >> args.shift  # --shift: smaller profiling cases (fewer, smaller joins)
     rng = np.random.default_rng(SEED)
-    r_sizes = np.exp(rng.uniform(np.log(2.0**10), np.log(2.0**20), size=joins)).astype(np.int64)
+    r_sizes = np.exp(rng.uniform(np.log(2.0**10), np.log(2.0 ** (20 - args.shift)), size=joins)).astype(np.int64)
     s_sizes = 4 * r_sizes
     r_off = np.concatenate([[0], np.cumsum(r_sizes)]).astype(np.int64)
     s_off = np.concatenate([[0], np.cumsum(s_sizes)]).astype(np.int64)
@@ -523,7 +523,7 @@ def run_batch_join(args) -> None:
     b_alg = n * (1 * (4 + 2 * 8) + 8) + m * 2 * 4
     peak, src = measured_peak()
     cfg = {
-        "workload": "batched join: 4096 int32 joins, |R_i| log-uniform [2^10, 2^20], |S_i| = 4|R_i|, 75% match, one vj_join_batch in a CUDA graph",
+        "workload": f"batched join: {joins} int32 joins, |R_i| log-uniform [2^10, 2^{20 - args.shift}], |S_i| = 4|R_i|, 75% match, one vj_join_batch in a CUDA graph",
         "joins": joins,
         "r_rows": nr,
         "s_rows": ns,
@@ -652,7 +652,7 @@ def run_hash_bench(args) -> None:
     oracle = _import(ROOT / "oracle" / "oracle.py", "vj_oracle")
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    n = 1 << 30
+    n = 1 << (30 - args.shift)  # --shift: smaller profiling cases
     peak, src = measured_peak()
     stream = torch.cuda.current_stream()
     gen = torch.Generator(device=dev)
@@ -679,7 +679,7 @@ def run_hash_bench(args) -> None:
         torch.cuda.empty_cache()
     clocks = sampler.stop()
     head = next(r for r in results if r["key_bytes"] == 16 and r["algo"] == "fnv")
-    cfg = {"workload": "hash 2^30 keys x {8,16,32} B, FNV-1a 64 and custom_xor_hw, 64-bit chunks", "keys": n, "l2_policy": "inputs 8-32 GiB, larger than L2"}
+    cfg = {"workload": f"hash 2^{30 - args.shift} keys x {{8,16,32}} B, FNV-1a 64 and custom_xor_hw, 64-bit chunks", "keys": n, "l2_policy": "inputs larger than L2"}
     line = _base_line("hash throughput (bytes read + written / s) on 1 GB300", head["GB/s"], "GB/s", args.steps, args.warmup, head["ms"], "u64", cfg)
     line["roofline"] = {"kernel": "hash_kernel", "bound": "hbm", "achieved": head["GB/s"], "peak": peak, "unit": "GB/s", "frac": head["frac"], "traffic": None, "peak_source": src}
     line["cases"] = results
