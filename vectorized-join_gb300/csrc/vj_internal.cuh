@@ -464,6 +464,7 @@ struct vj_ctx {
     bool events_ready;
     vj_profile last;         // filled after each join when profiling
     int launches;            // library kernels launched by the current join
+    int sm_reserve;          // SMs the join's kernels leave free (vj_join_host's copy kernels run there)
     std::vector<vj::TuneEntry> tuned;  // vj_tune results, consulted by automatic joins
 };
 

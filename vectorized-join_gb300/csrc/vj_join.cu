@@ -254,7 +254,12 @@ int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cu
     const uint32_t bins = 1u << P.bits;
     profile_mark(ctx, PM_PASS0 + 4 * pass, stream);
     VJ_TRY(pass_setup(P, b, stream));
-    histogram_kernel<KW, PB, HS, IN_AOS><<<b.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    if (ctx && ctx->sm_reserve) {
+        // SMs reserved: at most 4 blocks for each SM the join may use, looping over units
+        histogram_kernel<KW, PB, HS, IN_AOS, true><<<std::min(b.max_units, sms * 4), PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    } else {
+        histogram_kernel<KW, PB, HS, IN_AOS><<<b.max_units, PART_THREADS, bins * sizeof(uint32_t), stream>>>(P);
+    }
     VJ_CUDA(cudaGetLastError());
     profile_mark(ctx, PM_HIST_END + 4 * pass, stream);
     profile_mark(ctx, PM_SCAN_END + 4 * pass, stream);
@@ -272,11 +277,11 @@ int run_pass(vj_ctx *ctx, int sms, int pass, PassParams P, const PassBufs &b, cu
 }
 
 template <int KW, int PB, int HS, bool AOS, bool BATCH>
-int probe_grid(const DeviceInfo &info, int threads, size_t smem, int *grid) {
+int probe_grid(int sms, int threads, size_t smem, int *grid) {
     int per_sm = 0;
     VJ_TRY(blocks_per_sm(probe_kernel<KW, PB, HS, AOS, BATCH>, threads, smem, &per_sm));
     if (per_sm < 1) per_sm = 1;
-    *grid = info.sms * per_sm;
+    *grid = sms * per_sm;
     return VJ_OK;
 }
 
@@ -367,7 +372,7 @@ int probe_setup(vj_ctx *ctx, const Plan &pl, JoinRun *run) {
     run->threads = pl.threads;
     run->probe_smem = ProbeSmem<KW, PB, HS, AOS>::bytes(pl.rcap, pl.tcap, pl.scap);
     VJ_TRY(ensure_smem(probe_kernel<KW, PB, HS, AOS, BATCH>, run->probe_smem));
-    return probe_grid<KW, PB, HS, AOS, BATCH>(ctx->info, pl.threads, run->probe_smem, &run->probe_grid);
+    return probe_grid<KW, PB, HS, AOS, BATCH>(ctx->info.sms - ctx->sm_reserve, pl.threads, run->probe_smem, &run->probe_grid);
 }
 
 // Everything up to (not including) the probe launch. Returns probe parameters whose
@@ -1236,6 +1241,8 @@ namespace {
 // from host tables: 71.6 ms with 32, 75.7 with 16, no better with 64), and the other SMs
 // stay with the joins.
 constexpr int HOST_COPY_BLOCKS = 32;
+// SMs vj_join_host's joins leave to the copy kernels: both directions' blocks at 4 a SM
+constexpr int HOST_COPY_SMS = 2 * HOST_COPY_BLOCKS / 4;
 
 // Device address of host memory [p, p + bytes) that the GPU can load from (page-locked and
 // mapped, both ends in the same mapping), or null.
@@ -1415,10 +1422,10 @@ struct ChunkJoinerT final : ChunkJoiner {
                     P.next_plan = b.pb[1].plan;
                     P.next_max_units = b.pb[1].max_units;
                 }
-                VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, ctx->info.sms, pass, P, b.pb[0], stream)));
+                VJ_TRY((run_pass<KW, PB, HS, false, true>(ctx, ctx->info.sms - ctx->sm_reserve, pass, P, b.pb[0], stream)));
             } else {
                 P.plan = b.pb[1].plan;
-                VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, ctx->info.sms, pass, P, b.pb[1], stream)));
+                VJ_TRY((run_pass<KW, PB, HS, true, true>(ctx, ctx->info.sms - ctx->sm_reserve, pass, P, b.pb[1], stream)));
             }
             seg_begin = b.pb[pass].part_begin;
             seg_end = b.pb[pass].part_end;
@@ -1567,6 +1574,13 @@ int host_streams(vj_ctx *ctx) {
 int join_host_chunked(vj_ctx *ctx, const vj_table *r, const vj_table *s, const vj_join_options *options, void *h_pairs, uint64_t capacity, uint64_t *count, cudaStream_t st, int chunks, char *rk,
                       char *rp, char *sk, char *sp, char *dpairs) {
     VJ_TRY(host_streams(ctx));
+    // The join kernels leave HOST_COPY_SMS SMs to the copy kernels: persistent join kernels
+    // fill every SM's registers, and copy blocks that cannot start stall the host link.
+    struct Reserve {
+        vj_ctx *c;
+        explicit Reserve(vj_ctx *x) : c(x) { c->sm_reserve = std::min(HOST_COPY_SMS, c->info.sms / 4); }
+        ~Reserve() { c->sm_reserve = 0; }
+    } reserve(ctx);
     const size_t kb = (size_t)r->key_words * 4, pb = (size_t)r->payload_bytes;
     cudaEvent_t ev_start = ctx->host_ev[0], ev_in = ctx->host_ev[1], ev_out = ctx->host_ev[2], ev_r = ctx->host_ev[3];
     cudaEvent_t *ev_s = ctx->host_ev + 4, *ev_j = ctx->host_ev + 4 + 16;

@@ -656,12 +656,25 @@ __device__ __forceinline__ void histogram_unit(const PassParams &P, uint32_t u, 
 
 // Grid: one block per unit of the plan (blocks past the plan's units leave at once). Four
 // blocks per SM (32 registers a thread) keep enough loads in flight.
-template <int KW, int PB, int HS, bool AOS>
+// LOOP: a grid smaller than the plan (SMs left to other work) takes units blockIdx.x,
+// blockIdx.x + gridDim.x, ... (a separate instance: the loop costs the one-unit kernel
+// registers at its 32-register bound).
+template <int KW, int PB, int HS, bool AOS, bool LOOP = false>
 __global__ void __launch_bounds__(PART_THREADS, 4) histogram_kernel(PassParams P) {
     extern __shared__ uint32_t s_hist[];
     __shared__ HistShared sh;
-    if (blockIdx.x >= plan_total(P)) return;
-    histogram_unit<KW, PB, HS, AOS, PART_THREADS>(P, blockIdx.x, s_hist, sh);
+    if constexpr (LOOP) {
+        uint32_t u = blockIdx.x;
+        while (u < plan_total(P)) {
+            histogram_unit<KW, PB, HS, AOS, PART_THREADS>(P, u, s_hist, sh);
+            const uint32_t next = sh.u + gridDim.x;
+            __syncthreads();  // every thread has read sh.u before the next unit rewrites it
+            u = next;
+        }
+    } else {
+        if (blockIdx.x >= plan_total(P)) return;
+        histogram_unit<KW, PB, HS, AOS, PART_THREADS>(P, blockIdx.x, s_hist, sh);
+    }
 }
 
 // Shared memory of the scatter kernel: two input tiles filled by bulk copies, the
@@ -1538,13 +1551,23 @@ __device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s
                     uint32_t pos0 = 0;
                     if (lane == 0) pos0 = atomicAdd(&s_out_n[b], cnt);
                     pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+                    if (pos0 + cnt <= Q.scap) {
+                        // the warp's reservation fits the stage: no per-row overflow check
+                        // (one per row and round cost the probe 4.66 against 4.37 ms)
 #pragma unroll
-                    for (int j = 0; j < J; j++) {
-                        if (bal[j]) {
-                            const bool want = m[j] >= 0;
-                            const PT pr = Pair<PB>::make(want ? R.pay((uint32_t)m[j]) : Pt(0), rows[j].pay);
-                            stage_pairs<PB, BATCH>(Q, stage, pos0 + __popc(bal[j] & lt), want, pr, join, o_first, o_cap);
+                        for (int j = 0; j < J; j++) {
+                            if (m[j] >= 0) stage[pos0 + __popc(bal[j] & lt)] = Pair<PB>::make(R.pay((uint32_t)m[j]), rows[j].pay);
                             pos0 += __popc(bal[j]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < J; j++) {
+                            if (bal[j]) {
+                                const bool want = m[j] >= 0;
+                                const PT pr = Pair<PB>::make(want ? R.pay((uint32_t)m[j]) : Pt(0), rows[j].pay);
+                                stage_pairs<PB, BATCH>(Q, stage, pos0 + __popc(bal[j] & lt), want, pr, join, o_first, o_cap);
+                                pos0 += __popc(bal[j]);
+                            }
                         }
                     }
                 }
