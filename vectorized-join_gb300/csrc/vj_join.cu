@@ -72,28 +72,37 @@ uint32_t table_mul(int load_pct) {
 // SM slower still in the scatters), none shorter than MIN_UNIT_ROWS, and one more per
 // segment (every segment has a unit, whose block writes the segment's bounds).
 constexpr uint32_t MIN_UNIT_ROWS = 4096;
-int pass_units(const DeviceInfo &info, uint64_t rows, int G) {
+// Whole units cut in four at the end of a join's pass: two for each SM, so that the blocks
+// finishing the pass (two scatter blocks per SM) take quarter units.
+uint32_t tail_split(const DeviceInfo &info) { return 2u * (uint32_t)info.sms; }
+// split: the plan's whole units cut in four at its end (each adds three units)
+int pass_units(const DeviceInfo &info, uint64_t rows, int G, uint32_t split = 0) {
     const uint64_t by_rows = (rows + MIN_UNIT_ROWS - 1) / MIN_UNIT_ROWS;
     const uint64_t cap = (uint64_t)info.sms * 64;
-    return (int)((by_rows < cap ? by_rows : cap) + (uint64_t)G + 1);
+    return (int)((by_rows < cap ? by_rows : cap) + (uint64_t)G + 1 + 3ull * split);
 }
 
 // The unit plan of a pass over one or two whole tables (plan_block's rule, on the host).
 void host_plan(PassParams &P, const uint32_t *rows, int nsides) {
     uint64_t total = 0;
     for (int sd = 0; sd < nsides; sd++) total += rows[sd];
-    const uint64_t room = P.max_units > nsides ? (uint64_t)(P.max_units - nsides) : 1ull;
+    const uint64_t reserved = (uint64_t)nsides + 3ull * P.split;
+    const uint64_t room = (uint64_t)P.max_units > reserved ? (uint64_t)P.max_units - reserved : 1ull;
     uint64_t t = (total + room - 1) / room;
     if (t < P.min_unit_rows) t = P.min_unit_rows;
     if (t < 1) t = 1;
     const uint32_t target = (uint32_t)(t < 0x7fffffffull ? t : 0x7fffffffull);
-    P.plan = nullptr;
-    P.hplan[0] = target;
-    P.hplan[1] = 0;
+    uint32_t first[3] = {0, 0, 0};
     for (int sd = 0; sd < nsides; sd++) {
         const uint32_t n = rows[sd] ? (uint32_t)((rows[sd] + (uint64_t)target - 1) / target) : 1u;
-        P.hplan[2 + sd] = P.hplan[1 + sd] + n;
+        first[1 + sd] = first[sd] + n;
     }
+    const uint32_t units = first[nsides];
+    const uint32_t from = units - std::min(P.split, units / 4);
+    P.plan = nullptr;
+    P.hplan[0] = target;
+    for (int g = 0; g <= nsides; g++) P.hplan[1 + g] = split_index(first[g], from);
+    P.hplan[2 + nsides] = from;
 }
 
 template <int KW, int PB, int HS>
@@ -160,8 +169,8 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     for (int p = 0; p < 2; p++) {
         if (pl.bits[p] > MAX_RADIX_BITS) pl.bits[p] = MAX_RADIX_BITS;
     }
-    pl.max_units[0] = pass_units(info, nr + ns, 2);
-    pl.max_units[1] = pass_units(info, nr + ns, 2 << pl.bits[0]);
+    pl.max_units[0] = pass_units(info, nr + ns, 2, tail_split(info));
+    pl.max_units[1] = pass_units(info, nr + ns, 2 << pl.bits[0], tail_split(info));
     return pl;
 }
 
@@ -207,7 +216,7 @@ int blocks_per_sm(K kernel, int threads, size_t smem, int *per_sm) {
 
 // Bookkeeping of one pass (workspace).
 struct PassBufs {
-    uint32_t *plan = nullptr;              // [G + 2]: the pass's unit plan when the previous pass writes it
+    uint32_t *plan = nullptr;              // [G + 3]: the pass's unit plan when the previous pass writes it
     uint32_t *ctl = nullptr;               // [4]: counters and the scatter's ticket \  cleared
     uint32_t *seg_done = nullptr;          // [G]: units counted per segment          |  before
     uint32_t *seg_tot = nullptr;           // [G * bins]: bucket totals per segment   /  the pass
@@ -219,7 +228,7 @@ struct PassBufs {
 
 PassBufs carve_pass(Carver &c, int G, int bins, int max_units) {
     PassBufs b;
-    b.plan = c.take<uint32_t>((size_t)G + 2);
+    b.plan = c.take<uint32_t>((size_t)G + 3);
     b.ctl = c.take<uint32_t>(4);
     b.seg_done = c.take<uint32_t>((size_t)G, 16);
     b.seg_tot = c.take<uint32_t>((size_t)G * bins, 16);
@@ -388,8 +397,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
     const int np = J * (pl.passes == 0 ? 1 : (pl.passes == 1 ? bins0 : bins0 * bins1));
     int max_units[2] = {pl.max_units[0], pl.max_units[1]};
     if (batch) {
-        max_units[0] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G0);
-        max_units[1] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G1);
+        max_units[0] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G0, tail_split(ctx->info));
+        max_units[1] = pass_units(ctx->info, (uint64_t)in.rows[0] + in.rows[1], G1, tail_split(ctx->info));
     }
 
     // ---- workspace layout (dry run, then carve): per pass one row-contiguous buffer per side
@@ -482,6 +491,8 @@ int prepare(vj_ctx *ctx, const Tables &in, const Plan &pl, const HashSpec &hs, c
         P.hs = hs;
         P.max_units = max_units[pass];
         P.min_unit_rows = MIN_UNIT_ROWS;
+        P.split = tail_split(ctx->info);
+        P.next_split = tail_split(ctx->info);
         P.error = error;
         const PassBufs &pb = pass == 0 ? pb0 : pb1;
         if (pass == 0 && !batch) {
@@ -1373,7 +1384,7 @@ struct ChunkJoinerT final : ChunkJoiner {
         b->bids = pl.passes >= 2 ? c.take<uint16_t>((size_t)rows + 8) : nullptr;
         for (int pass = 0; pass < pl.passes; pass++) {
             const int G = pass == 0 ? 1 : 1 << pl.bits[0];
-            b->pb[pass] = carve_pass(c, G, 1 << pl.bits[pass], pass_units(ctx->info, rows, G));
+            b->pb[pass] = carve_pass(c, G, 1 << pl.bits[pass], pass_units(ctx->info, rows, G, tail_split(ctx->info)));
         }
     }
 
@@ -1415,6 +1426,8 @@ struct ChunkJoinerT final : ChunkJoiner {
             P.hs = hs;
             P.max_units = b.pb[pass].max_units;
             P.min_unit_rows = MIN_UNIT_ROWS;
+            P.split = tail_split(ctx->info);
+            P.next_split = tail_split(ctx->info);
             P.error = error;
             if (pass == 0) {
                 host_plan(P, &rows, 1);

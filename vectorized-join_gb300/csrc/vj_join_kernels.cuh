@@ -76,12 +76,14 @@ struct PassParams {
     int next_shift, next_bits;   // bucket of the next pass (bid_out)
     // Units: segment g's rows are cut into units of `target` rows (its last one shorter, at
     // least one unit per segment); units [first[g], first[g + 1]) belong to segment g. The
-    // plan (target, first[0..G]) is `plan` on the device or, when plan is null, hplan
-    // (G <= 2, planned on the host).
+    // last units of the pass are cut in four (split_plan): units from `split_from` on are
+    // quarters of the units they replace. The plan (target, first[0..G], split_from) is
+    // `plan` on the device or, when plan is null, hplan (G <= 2, planned on the host).
     const uint32_t *plan;
-    uint32_t hplan[4];
+    uint32_t hplan[5];
     int max_units;
     uint32_t min_unit_rows;
+    uint32_t split;              // units to cut in four at the end of the pass (0: none)
     uint32_t *ctl;               // [4], zero before the pass: units counted, scatter ticket
     uint32_t *seg_done;          // [G], zero before the pass: units counted per segment
     uint32_t *seg_tot;           // [G*bins], zero before the pass: the segments' bucket totals
@@ -90,8 +92,9 @@ struct PassParams {
     uint32_t *part_end;          // [G*bins]
     uint32_t *error;             // bit 4: a bulk-copy wait ran out
     // the next pass's plan over this pass's partitions (written by the unit counted last)
-    uint32_t *next_plan;         // [G*bins + 2] or null
+    uint32_t *next_plan;         // [G*bins + 3] or null
     int next_max_units;
+    uint32_t next_split;
 };
 
 struct ProbeParams {
@@ -402,6 +405,7 @@ __device__ __forceinline__ UnitRange unit_range(const PassParams &P, uint32_t u)
     const uint32_t G = (uint32_t)(P.nsides * P.Q);
     const uint32_t *first = plan_first(P);
     const uint32_t target = P.plan ? P.plan[0] : P.hplan[0];
+    const uint32_t from = first[G + 1];  // the first quarter unit
     uint32_t lo = 0, hi = G - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
@@ -414,20 +418,36 @@ __device__ __forceinline__ UnitRange unit_range(const PassParams &P, uint32_t u)
     r.side = g / (uint32_t)P.Q;
     const uint32_t sb = P.seg_begin ? P.seg_begin[g] : 0;
     const uint32_t se = P.seg_end ? P.seg_end[g] : P.side[r.side].rows;
-    const unsigned long long a = (unsigned long long)sb + (unsigned long long)(u - f0) * target;
-    r.a = (uint32_t)(a < se ? a : se);
-    r.b = (uint32_t)(a + target < se ? a + target : se);
+    // the whole unit it is (or a quarter of): index in the plan before the split
+    const uint32_t whole = u < from ? u : from + (u - from) / 4;
+    const uint32_t seg0 = f0 <= from ? f0 : from + (f0 - from) / 4;
+    const unsigned long long a = (unsigned long long)sb + (unsigned long long)(whole - seg0) * target;
+    unsigned long long ra = a < se ? a : se;
+    unsigned long long rb = a + target < se ? a + target : se;
+    if (u >= from) {
+        const unsigned long long len = rb - ra, q = (u - from) & 3u;
+        rb = ra + len * (q + 1) / 4;
+        ra = ra + len * q / 4;
+    }
+    r.a = (uint32_t)ra;
+    r.b = (uint32_t)rb;
     r.rank = u - f0;
     r.first = u == f0;
     r.last = u + 1 == f1;
     return r;
 }
 
+// Units from `from` on (the last `split` whole units of the plan, in unit order) become four
+// quarter units each: unit index x of the whole-unit plan maps to split_index(x).
+__host__ __device__ __forceinline__ uint32_t split_index(uint32_t x, uint32_t from) { return x <= from ? x : from + 4 * (x - from); }
+
 // One block: units of `target` rows for the G segments [begin[g], end[g]) -- at least one per
 // segment, so that every segment's bounds are written by its last unit. plan[0] = target,
-// plan[1 + g] = the first unit of g, plan[1 + G] = all units. target is the larger of
-// min_rows and the rows that spread the segments over max_units - G units.
-static __device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t G, uint32_t max_units, uint32_t min_rows, uint32_t *plan) {
+// plan[1 + g] = the first unit of g, plan[1 + G] = all units, plan[2 + G] = the first quarter
+// unit: the last min(split, units / 4) whole units are cut in four, so that blocks finishing
+// a pass take short units (its tail shrinks by as much). target is the larger of min_rows
+// and the rows that spread the segments over max_units - G - 3 split units.
+static __device__ void plan_block(const uint32_t *begin, const uint32_t *end, uint32_t G, uint32_t max_units, uint32_t min_rows, uint32_t split, uint32_t *plan) {
     __shared__ unsigned long long s_w64[32];
     __shared__ uint32_t s_w32[32];
     __shared__ uint32_t s_target;
@@ -438,7 +458,7 @@ static __device__ void plan_block(const uint32_t *begin, const uint32_t *end, ui
     unsigned long long total = 0;
     block_exclusive_scan<unsigned long long>(rows, s_w64, &total);
     if (threadIdx.x == 0) {
-        const unsigned long long room = max_units > G ? (unsigned long long)(max_units - G) : 1ull;
+        const unsigned long long room = max_units > G + 3 * split ? (unsigned long long)(max_units - G - 3 * split) : 1ull;
         unsigned long long t = (total + room - 1) / room;
         if (t < min_rows) t = min_rows;
         if (t < 1) t = 1;
@@ -454,20 +474,22 @@ static __device__ void plan_block(const uint32_t *begin, const uint32_t *end, ui
     }
     uint32_t units = 0;
     uint32_t run = block_exclusive_scan<uint32_t>(mine, s_w32, &units);
+    const uint32_t from = units - min(split, units / 4);
     for (uint32_t g = g0; g < g0 + per && g < G; g++) {
-        plan[1 + g] = run;
+        plan[1 + g] = split_index(run, from);
         const uint32_t n = end[g] - begin[g];
         run += n ? (n + target - 1) / target : 1u;
     }
     if (threadIdx.x == 0) {
         plan[0] = target;
-        plan[1 + G] = units;
+        plan[1 + G] = split_index(units, from);
+        plan[2 + G] = from;
     }
 }
 
 // One block: the unit plan of a pass over device segments (batches of joins).
 static __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(PassParams P, uint32_t *plan) {
-    plan_block(P.seg_begin, P.seg_end, (uint32_t)(P.nsides * P.Q), (uint32_t)P.max_units, P.min_unit_rows, plan);
+    plan_block(P.seg_begin, P.seg_end, (uint32_t)(P.nsides * P.Q), (uint32_t)P.max_units, P.min_unit_rows, P.split, plan);
 }
 
 // L2 prefetch of what the histogram reads of rows [a, b): the hash or key column, or the rows.
@@ -653,7 +675,7 @@ __device__ __forceinline__ void histogram_unit(const PassParams &P, uint32_t u, 
         __syncthreads();
         if (sh.last) {
             __threadfence();
-            plan_block(P.part_begin, P.part_end, (uint32_t)(P.nsides * P.Q) * bins, (uint32_t)P.next_max_units, P.min_unit_rows, P.next_plan);
+            plan_block(P.part_begin, P.part_end, (uint32_t)(P.nsides * P.Q) * bins, (uint32_t)P.next_max_units, P.min_unit_rows, P.next_split, P.next_plan);
         }
     }
 }
@@ -1776,7 +1798,7 @@ __global__ void __launch_bounds__(PROBE_THREADS, 1) batch_fused_kernel(BatchFuse
     if (!grid_sync(F.sync, error)) return;
     if (blockIdx.x == 0) {
         out_monotone_block(F.joins, F.out_begin);
-        if (AOS) plan_block(F.seg_begin, F.seg_end, 2 * F.joins, (uint32_t)F.P.max_units, F.P.min_unit_rows, F.plan);
+        if (AOS) plan_block(F.seg_begin, F.seg_end, 2 * F.joins, (uint32_t)F.P.max_units, F.P.min_unit_rows, F.P.split, F.plan);
     }
     if (!grid_sync(F.sync, error)) return;
     if (AOS) {
