@@ -365,6 +365,26 @@ __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.w
 // The issuing thread's bulk stores are complete.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// Stores under an L2 evict-last policy. A partition pass writes each bucket's rows as
+// runs that start at any 16-byte offset, so a run's first and last 32-byte sectors are
+// only partly written until the next tile's run of the same bucket completes them; kept in
+// L2 until then, they go to HBM once and whole instead of being read back and merged (for
+// the 2^27 x 2^29 join the two scatter passes went from 6.05 + 5.22 to 5.84 + 5.02 ms).
+__device__ __forceinline__ uint64_t l2_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void st_evict_last(void *p, const uint4 &v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_evict_last(void *p, const uint2 &v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(p), "r"(v.x), "r"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_evict_last(uint16_t *p, uint16_t v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.u16 [%0], %1, %2;" ::"l"(p), "h"(v), "l"(pol) : "memory");
+}
+
 // Prefetch [src, src + bytes) into L2 through the bulk-copy engine (no completion to wait
 // for; src 16-byte aligned, bytes a multiple of 16).
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
