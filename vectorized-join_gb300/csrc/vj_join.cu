@@ -122,7 +122,7 @@ Plan make_plan(uint64_t nr, uint64_t ns, const DeviceInfo &info, const vj_join_o
     for (uint32_t rcap = 2048; rcap >= 64; rcap >>= 1) {
         uint32_t tcap = 64;
         while (tcap < rcap * pl.tmul) tcap <<= 1;
-        if (tcap <= 16384 && SMf::bytes(rcap, tcap, rcap) <= budget) {
+        if (tcap <= (1u << SLOT_BITS) && SMf::bytes(rcap, tcap, rcap) <= budget) {
             pl.rcap = rcap;
             break;
         }
