@@ -110,6 +110,44 @@ def test_degenerate_hash_one_partition(vjlib, ctx, cuda, oracle):
     assert np.array_equal(sort_pairs(got), want)
 
 
+@pytest.mark.parametrize("pattern", ["high_word", "equal_halves", "top_bits", "stride_2p20", "int32_high", "wide_last_word"])
+def test_patterned_keys_vs_oracle(vjlib, ctx, cuda, oracle, pattern):
+    # Keys whose differences sit in few bits: the probe's table slots come from a
+    # multiplicative mix of the key (not of its hash), so such key sets must still find
+    # every match, whatever the partitioning.
+    rng = np.random.default_rng(11)
+    n = 12_000
+    i = rng.permutation(n).astype(np.uint64) + np.uint64(1)
+    if pattern == "high_word":
+        rk = i << np.uint64(32)
+    elif pattern == "equal_halves":
+        rk = (i << np.uint64(32)) | i
+    elif pattern == "top_bits":
+        rk = i << np.uint64(50)
+    elif pattern == "stride_2p20":
+        rk = i << np.uint64(20)
+    elif pattern == "int32_high":
+        rk = (i << np.uint64(18)).astype(np.uint32)
+    else:  # 16-byte keys equal but for the last word
+        rk = np.zeros((n, 2), dtype=np.uint64)
+        rk[:, 0] = np.uint64(0x0123456789ABCDEF)
+        rk[:, 1] = i << np.uint64(40)
+    pick = rng.integers(0, n, size=3 * n)
+    sk = rk[pick].copy()
+    miss = rng.random(3 * n) < 0.3  # 30 % of the probe rows get a key outside R
+    if rk.ndim == 1:
+        sk[miss] = sk[miss] + rk.dtype.type(1)
+    else:
+        sk[miss, 0] = sk[miss, 0] + np.uint64(1)
+    rp = np.arange(n, dtype=np.uint64)
+    sp = np.arange(3 * n, dtype=np.uint64)
+    cnt, want, _ = oracle.join(rk, rp, sk, sp)
+    for opts in (None, vjlib.options(passes=0), vjlib.options(passes=1, radix_bits=(3, 0))):
+        count, got = gpu_join(vjlib, ctx, cuda, rk, rp, sk, sp, opts, capacity=max(1, cnt))
+        assert count == cnt, (pattern, opts)
+        assert np.array_equal(sort_pairs(got), want), (pattern, opts)
+
+
 def test_skewed_probe_side(vjlib, ctx, cuda, oracle):
     rng = np.random.default_rng(5)
     nr, ns = 50_000, 400_000

@@ -67,10 +67,12 @@ uint32_t table_mul(int load_pct) {
     return m;
 }
 
-// Units of a pass over `rows` rows in G segments: at most 64 per SM (short units keep the
-// SMs busy as blocks finish; 16 per SM was 0.26 ms slower on the 2^27 x 2^29 join, 256 per
-// SM slower still in the scatters), none shorter than MIN_UNIT_ROWS, and one more per
-// segment (every segment has a unit, whose block writes the segment's bounds).
+// Units of a pass over `rows` rows in G segments: at most 48 per SM (short units keep the
+// SMs busy as blocks finish, but each unit publishes a look-back word per bucket; on the
+// 2^27 x 2^29 join 48 per SM took 15.71 ms against 15.80 with 64 and 15.74 with 32, and 16
+// per SM, before the pass tails were cut in quarter units, 0.26 ms more than 64), none
+// shorter than MIN_UNIT_ROWS, and one more per segment (every segment has a unit, whose
+// block writes the segment's bounds).
 constexpr uint32_t MIN_UNIT_ROWS = 4096;
 // Whole units cut in four at the end of a join's pass: two for each SM, so that the blocks
 // finishing the pass (two scatter blocks per SM) take quarter units.
@@ -78,7 +80,7 @@ uint32_t tail_split(const DeviceInfo &info) { return 2u * (uint32_t)info.sms; }
 // split: the plan's whole units cut in four at its end (each adds three units)
 int pass_units(const DeviceInfo &info, uint64_t rows, int G, uint32_t split = 0) {
     const uint64_t by_rows = (rows + MIN_UNIT_ROWS - 1) / MIN_UNIT_ROWS;
-    const uint64_t cap = (uint64_t)info.sms * 64;
+    const uint64_t cap = (uint64_t)info.sms * 48;
     return (int)((by_rows < cap ? by_rows : cap) + (uint64_t)G + 1 + 3ull * split);
 }
 
