@@ -608,8 +608,8 @@ __device__ __forceinline__ void histogram_unit(const PassParams &P, uint32_t u, 
                 }
             });
     } else if (!AOS && HS == 0 && KW <= 2 && ((uintptr_t)S.keys_in & 15) == 0) {
-        // 4- or 8-byte keys, 4 or 2 a load
-        count_groups<NT, 4 / KW>(S.keys_in, U.a, U.b, count_row, [&](const uint4 &v) {
+        // 4- or 8-byte keys, 4 or 2 a load (the group size of wider keys is never used)
+        count_groups<NT, (KW <= 2 ? 4 / KW : 1)>(S.keys_in, U.a, U.b, count_row, [&](const uint4 &v) {
             const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int k = 0; k < 4; k += KW) {
