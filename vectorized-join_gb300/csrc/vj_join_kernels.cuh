@@ -1565,6 +1565,8 @@ __device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s
         // rows past the first NC land on the last warps, while the probe rows past a whole
         // number of rounds land on the first ones, so no warp carries both extras to the
         // table barrier (4.81 -> 4.54 ms for the 2^27 x 2^29 join's probe).
+        // one probe row's load before the build, the first round's others after it (below)
+        if (c < ns) load_probe<KW, PB, HS, AOS>(Q, d.z + c, rows[0]);
         bool dup = false;
         for (uint32_t i = NC - 1 - c; i < nr; i += NC) {
             const Key<KW> key = R.key(i);
@@ -1588,11 +1590,13 @@ __device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s
             }
         }
         if (dup) s_dups[b] = tag;
-        // first round of probe rows, issued after the build: they are in flight during the
-        // table barrier, and the build no longer waits behind ~5000 loads queued at once
-        // (the 2^27 x 2^29 join's probe: 4.33 -> 4.03 ms)
+        // the rest of the first round of probe rows, issued after the build: they are in
+        // flight during the table barrier, and the build does not wait behind ~5000 loads
+        // queued at once (the 2^27 x 2^29 join's probe: all five before the build 4.33 ms,
+        // all after 4.03; with key-only loads all after 3.604, one before 3.584, two 3.586,
+        // three 3.66)
 #pragma unroll
-        for (int j = 0; j < J; j++) {
+        for (int j = 1; j < J; j++) {
             const uint32_t i = c + (uint32_t)j * NC;
             if (i < ns) load_probe<KW, PB, HS, AOS>(Q, d.z + i, rows[j]);
         }
