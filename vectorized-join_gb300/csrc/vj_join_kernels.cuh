@@ -1566,8 +1566,10 @@ __device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s
         // rows past the first NC land on the last warps, while the probe rows past a whole
         // number of rounds land on the first ones, so no warp carries both extras to the
         // table barrier (4.81 -> 4.54 ms for the 2^27 x 2^29 join's probe).
-        // one probe row's load before the build, the first round's others after it (below)
-        if (c < ns) load_probe<KW, PB, HS, AOS>(Q, d.z + c, rows[0]);
+        // one probe row's load before the build, the first round's others after it (below);
+        // batches issue all five after it (the fused batch launch: 45.7 against 45.1 ms with
+        // one before)
+        if (!BATCH && c < ns) load_probe<KW, PB, HS, AOS>(Q, d.z + c, rows[0]);
         bool dup = false;
         for (uint32_t i = NC - 1 - c; i < nr; i += NC) {
             const Key<KW> key = R.key(i);
@@ -1597,7 +1599,7 @@ __device__ __forceinline__ void probe_run(const ProbeParams &Q, unsigned char *s
         // all after 4.03; with key-only loads all after 3.604, one before 3.584, two 3.586,
         // three 3.66)
 #pragma unroll
-        for (int j = 1; j < J; j++) {
+        for (int j = BATCH ? 0 : 1; j < J; j++) {
             const uint32_t i = c + (uint32_t)j * NC;
             if (i < ns) load_probe<KW, PB, HS, AOS>(Q, d.z + i, rows[j]);
         }
