@@ -292,6 +292,30 @@ def test_build_probe_with_and_without_hashes(vjlib, ctx, cuda, oracle):
     assert ctx.build_probe(t_r, t_s, out=None, capacity=0) == cnt
 
 
+def test_build_probe_partitioned_with_hashes(vjlib, ctx, cuda, oracle):
+    # tables large enough that build_and_probe partitions them: the probe reads row-contiguous
+    # rows that carry their hash (key and hash loaded, the payload read when a row matches)
+    import torch
+
+    rng = np.random.default_rng(9)
+    nr, ns = 60_000, 200_000
+    rk = rng.integers(0, 80_000, size=nr, dtype=np.uint64)
+    sk = rng.integers(0, 80_000, size=ns, dtype=np.uint64)
+    rp = np.arange(1, nr + 1, dtype=np.uint64)
+    sp = np.arange(1, ns + 1, dtype=np.uint64)
+    cnt, want, _ = oracle.join(rk, rp, sk, sp)
+    out = torch.zeros((max(cnt, 1), 2), dtype=torch.int64, device=cuda)
+    t_r = vjlib.table(dev(rk, cuda), dev(rp, cuda), nr, 2, 8)
+    t_s = vjlib.table(dev(sk, cuda), dev(sp, cuda), ns, 2, 8)
+    for hb in (32, 64):
+        rh, _ = oracle.hash_elements(rk.view(np.uint32), nr, 0, 1, 64, hb, "fnv")
+        sh, _ = oracle.hash_elements(sk.view(np.uint32), ns, 0, 1, 64, hb, "fnv")
+        out.zero_()
+        n = ctx.build_probe(t_r, t_s, r_hashes=dev(rh, cuda), s_hashes=dev(sh, cuda), hash_bits=hb, out=out, capacity=cnt)
+        assert n == cnt, hb
+        assert np.array_equal(sort_pairs(out[:n].cpu().numpy().view(np.uint64)), want), hb
+
+
 def test_generator_matches_oracle(vjlib, cuda, oracle):
     import torch
 

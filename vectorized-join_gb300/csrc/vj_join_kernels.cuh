@@ -1300,13 +1300,14 @@ __device__ __forceinline__ void load_probe_row(const ProbeParams &Q, uint32_t s,
     }
 }
 
-// Probe rows in a row-contiguous buffer (no hashes carried) are loaded key only, through L1
-// (the probe walk needs nothing else); a matching row's payload is read from the same row
-// when its pair is staged, mostly an L1 or L2 hit. Holding five rows' payloads in registers
-// through the walk made the probe spill (2^27 x 2^29 int64 join's probe: 3.77 -> 3.61 ms).
+// Probe rows in a row-contiguous buffer are loaded without their payload (key, and the hash
+// where rows carry one), through L1 -- the probe walk needs nothing else; a matching row's
+// payload is read from the same row when its pair is staged, mostly an L1 or L2 hit.
+// Holding five rows' payloads in registers through the walk made the probe spill
+// (2^27 x 2^29 int64 join's probe: 3.77 -> 3.61 ms).
 template <int KW, int PB, int HS, bool AOS>
 constexpr bool probe_key_only() {
-    return AOS && HS == 0;
+    return AOS;
 }
 template <int KW, int PB, int HS>
 __device__ __forceinline__ void load_probe_key(const ProbeParams &Q, uint32_t s, ProbeRow<KW, PB, HS> &r) {
@@ -1324,7 +1325,9 @@ __device__ __forceinline__ void load_probe_key(const ProbeParams &Q, uint32_t s,
         for (int i = 0; i < KW; i++) r.key.w[i] = *((const uint32_t *)p + i);
     }
     r.pay = 0;
-    r.hash = 0;
+    if constexpr (HS == 8) r.hash = *(const unsigned long long *)(p + Layout<KW, PB, HS>::HASH_OFF);
+    else if constexpr (HS == 4) r.hash = *(const uint32_t *)(p + Layout<KW, PB, HS>::HASH_OFF);
+    else r.hash = 0;
 }
 template <int KW, int PB, int HS, bool AOS>
 __device__ __forceinline__ void load_probe(const ProbeParams &Q, uint32_t s, ProbeRow<KW, PB, HS> &r) {
