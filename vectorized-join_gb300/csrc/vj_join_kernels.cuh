@@ -1231,7 +1231,7 @@ struct Pair<8> {
 //   consumers, item k:
 //     wait full[b]; insert the build rows into table[b] (u16 slots: tag << 11 | row,
 //     atomicCAS, the slot from a mix of the key: table_slot); load their first probe rows
-//     into registers (key only for row-contiguous rows; in flight at the barrier)
+//     into registers (without payloads for row-contiguous rows; in flight at the barrier)
 //     named barrier over the consumers: the table is complete (the only block-level wait)
 //     probe: rows straight from global memory, J per thread per round, matches staged per
 //     item in stage[b] (one shared-memory reservation per warp and round)
